@@ -1,0 +1,248 @@
+"""ORACLE (test infrastructure only): Python front end of the CPU restatements.
+
+What is here, and the reference code each piece follows (paths inside lean-fftw):
+
+* `ref_transform`      refTransform / stockhamWith / passWith (Gen/Stockham.lean:263-301):
+                       the binary64 Stockham passes the reference's fast engine reproduces
+                       bit for bit; twiddle tables from `trig_ref` (Core/Trig.lean:131-134,
+                       Core/FastPlan.lean:163-183).
+* `generic_dft`        the generic engine, exec floatOps (mkPlan floatOps fwd
+                       (primeFactors n)) (Core/Alg.lean:236-254, Core/Problem.lean:126-127).
+* `generic_r2c/c2r`    LineOp.apply for r2c and c2r (Core/Problem.lean:142-150, hermExt :137).
+* `generic_rank2_r2c`  planProblemCore for rdft2 forward, rank 2 (Core/Problem.lean:228-233):
+                       r2c along the last axis, then a complex forward DFT along the first.
+* `dd_dft`             extended-precision (double-double) DFT: the accuracy oracle.
+* `lcg_rand`           randArr of scripts/AsmTest.lean:7-13, the reference tests' inputs.
+
+The reference engine itself cannot run here: it needs a Lean 4.35 toolchain (absent, no
+network) and AVX-512 (absent on aarch64 hosts).  Parity is pinned instead through the
+reference's published known answers (see tests/test_oracle_pins.py).
+
+Only tests, the smoke check and the CPU-baseline leg of the benchmark may import this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+from functools import lru_cache
+from typing import List, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import trig_ref  # noqa: E402
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+@lru_cache(maxsize=1)
+def lib() -> ctypes.CDLL:
+    so = os.path.join(HERE, "_build", "liboracle.so")
+    if not os.path.exists(so):
+        import build_oracle
+        build_oracle.build()
+    L = ctypes.CDLL(so)
+    L.lfo_ref_transform.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.POINTER(ctypes.c_int),
+                                    ctypes.c_int, ctypes.POINTER(_dp), _dp, _dp, ctypes.c_long,
+                                    ctypes.c_int]
+    L.lfo_ref_transform.restype = ctypes.c_int
+    L.lfo_generic_dft.argtypes = [ctypes.c_int, ctypes.c_long, _dp, _dp, ctypes.c_long,
+                                  ctypes.c_long, _dp, ctypes.c_long, ctypes.c_long,
+                                  ctypes.c_long, ctypes.c_int]
+    L.lfo_generic_dft.restype = ctypes.c_int
+    L.lfo_dd_dft.argtypes = [ctypes.c_int, ctypes.c_long, _dp, _dp, ctypes.c_long, ctypes.c_long,
+                             _dp, _dp, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_int]
+    L.lfo_dd_dft.restype = ctypes.c_int
+    L.lfo_rel_l2.argtypes = [_dp, _dp, _dp, ctypes.c_long]
+    L.lfo_rel_l2.restype = ctypes.c_double
+    return L
+
+
+def _p(a: np.ndarray):
+    assert a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def nthreads_default() -> int:
+    return max(1, min(os.cpu_count() or 1, 16))
+
+
+# ------------------------------------------------------------------ twiddles
+
+def pass_ns(rs: Sequence[int], t: int) -> int:
+    """Product of the radices before pass t (FastPlan.lean:158)."""
+    p = 1
+    for r in rs[:t]:
+        p *= r
+    return p
+
+
+@lru_cache(maxsize=64)
+def _plan_twiddles(fwd: bool, N: int, rs: tuple):
+    tab = trig_ref.table(N)
+    out = [np.zeros(1)]
+    for t in range(1, len(rs)):
+        out.append(np.ascontiguousarray(
+            trig_ref.pass_twiddles(tab, fwd, N, rs[t], pass_ns(rs, t)), dtype=np.float64))
+    return out
+
+
+def plan_twiddles(fwd: bool, N: int, rs: Sequence[int]) -> List[np.ndarray]:
+    """Twiddle table of every pass t >= 1 (entry 0 unused)."""
+    return _plan_twiddles(bool(fwd), int(N), tuple(int(r) for r in rs))
+
+
+@lru_cache(maxsize=64)
+def _tab_array(n: int) -> np.ndarray:
+    return np.ascontiguousarray(np.array(trig_ref.table(n), dtype=np.float64).reshape(-1))
+
+
+@lru_cache(maxsize=64)
+def _dd_tab_array(n: int) -> np.ndarray:
+    return np.ascontiguousarray(np.array(trig_ref.dd_table(n), dtype=np.float64).reshape(-1))
+
+
+# ------------------------------------------------------------------ transforms
+
+def _as_batch(x: np.ndarray, N: int) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    return x.reshape(-1, N)
+
+
+def ref_transform(fwd: bool, N: int, rs: Sequence[int], x: np.ndarray,
+                  nthreads: int = 1) -> np.ndarray:
+    """refTransform fwd N rs on each row of x (complex128, last axis N)."""
+    rs = [int(r) for r in rs]
+    assert int(np.prod(rs)) == N, (N, rs)
+    shape = x.shape
+    xb = _as_batch(x, N)
+    out = np.empty_like(xb)
+    tws = plan_twiddles(fwd, N, rs)
+    arr = (_dp * len(rs))(*[_p(t) for t in tws])
+    rsa = (ctypes.c_int * len(rs))(*rs)
+    xin = xb.view(np.float64)
+    xo = out.view(np.float64)
+    rc = lib().lfo_ref_transform(int(fwd), N, rsa, len(rs), arr, _p(xin), _p(xo), xb.shape[0],
+                                 nthreads)
+    assert rc == 0, "reference transform failed (radix without a codelet?)"
+    return out.reshape(shape)
+
+
+def generic_dft(fwd: bool, x: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    """The generic engine's 1-D DFT along the last axis."""
+    N = x.shape[-1]
+    xb = _as_batch(x, N)
+    out = np.empty_like(xb)
+    lib().lfo_generic_dft(int(fwd), N, _p(_tab_array(N)), _p(xb.view(np.float64)), 1, N,
+                          _p(out.view(np.float64)), 1, N, xb.shape[0], nthreads)
+    return out.reshape(x.shape)
+
+
+def dd_dft(fwd: bool, x: np.ndarray, nthreads: int = 1):
+    """Double-double DFT along the last axis: returns (hi, lo) complex128 arrays whose sum
+    is the transform to about 106 bits."""
+    N = x.shape[-1]
+    xb = _as_batch(x, N)
+    hi = np.empty_like(xb)
+    lo = np.empty_like(xb)
+    lib().lfo_dd_dft(int(fwd), N, _p(_dd_tab_array(N)), _p(xb.view(np.float64)), 1, N,
+                     _p(hi.view(np.float64)), _p(lo.view(np.float64)), 1, N, xb.shape[0],
+                     nthreads)
+    return hi.reshape(x.shape), lo.reshape(x.shape)
+
+
+def rel_l2(y: np.ndarray, ref) -> float:
+    """Relative L2 error ||y - ref|| / ||ref||, ref = (hi, lo) double-double or an array."""
+    if isinstance(ref, tuple):
+        hi, lo = ref
+    else:
+        hi, lo = ref, np.zeros_like(ref)
+    yv = np.ascontiguousarray(y).reshape(-1).view(np.float64) if np.iscomplexobj(y) else \
+        np.ascontiguousarray(y, dtype=np.float64).reshape(-1)
+    hv = np.ascontiguousarray(hi).reshape(-1)
+    lv = np.ascontiguousarray(lo).reshape(-1)
+    if np.iscomplexobj(hv):
+        hv, lv = hv.view(np.float64), lv.view(np.float64)
+    return float(lib().lfo_rel_l2(_p(yv), _p(np.ascontiguousarray(hv)),
+                                  _p(np.ascontiguousarray(lv)), yv.size))
+
+
+# ------------------------------------------------------------------ real transforms
+
+def herm_ext(h: np.ndarray, n: int) -> np.ndarray:
+    """Hermitian extension of the half spectrum (Problem.lean:137-138)."""
+    full = np.empty(h.shape[:-1] + (n,), dtype=np.complex128)
+    full[..., : n // 2 + 1] = h[..., : n // 2 + 1]
+    k = np.arange(n // 2 + 1, n)
+    full[..., k] = np.conj(h[..., n - k])
+    return full
+
+
+def generic_r2c(x: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    """r2c by the generic engine (Problem.lean:145-147)."""
+    n = x.shape[-1]
+    F = generic_dft(True, x.astype(np.complex128), nthreads)
+    return np.ascontiguousarray(F[..., : n // 2 + 1])
+
+
+def generic_c2r(h: np.ndarray, n: int, nthreads: int = 1) -> np.ndarray:
+    """c2r by the generic engine (Problem.lean:148-150): the imaginary parts of the
+    self-conjugate entries are ignored through the Hermitian extension."""
+    G = generic_dft(False, herm_ext(h, n), nthreads)
+    return np.ascontiguousarray(G.real)
+
+
+def generic_rank2_r2c(x: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    """Rank-2 rdft2 forward (Problem.lean:228-233) on x of shape (..., n0, n1)."""
+    h = generic_r2c(x, nthreads)                       # (..., n0, n1/2+1)
+    ht = np.ascontiguousarray(np.swapaxes(h, -1, -2))  # (..., n1/2+1, n0)
+    return np.ascontiguousarray(np.swapaxes(generic_dft(True, ht, nthreads), -1, -2))
+
+
+def dd_r2c(x: np.ndarray, nthreads: int = 1):
+    n = x.shape[-1]
+    hi, lo = dd_dft(True, x.astype(np.complex128), nthreads)
+    return (np.ascontiguousarray(hi[..., : n // 2 + 1]), np.ascontiguousarray(lo[..., : n // 2 + 1]))
+
+
+def dd_c2r(h: np.ndarray, n: int, nthreads: int = 1):
+    hi, lo = dd_dft(False, herm_ext(h, n), nthreads)
+    return np.ascontiguousarray(hi.real), np.ascontiguousarray(lo.real)
+
+
+def dd_rank2_r2c(x: np.ndarray, nthreads: int = 1):
+    """Rank-2 r2c in double-double: dd rows, then dd columns (the column pass takes the
+    rounded row result, whose rounding error is ~1e-32 relative, far below binary64)."""
+    n1 = x.shape[-1]
+    hi, lo = dd_dft(True, x.astype(np.complex128), nthreads)
+    hi, lo = hi[..., : n1 // 2 + 1], lo[..., : n1 // 2 + 1]
+    ht = np.ascontiguousarray(np.swapaxes(hi, -1, -2))
+    lt = np.ascontiguousarray(np.swapaxes(lo, -1, -2))
+    h2, l2 = dd_dft(True, ht, nthreads)
+    h3, _ = dd_dft(True, lt, nthreads)
+    # DFT is linear: DFT(hi) + DFT(lo); DFT(lo) is ~1e-16 smaller, so its own binary64
+    # evaluation error is ~1e-32 relative to the result.
+    return (np.ascontiguousarray(np.swapaxes(h2, -1, -2)),
+            np.ascontiguousarray(np.swapaxes(l2 + h3, -1, -2)))
+
+
+# ------------------------------------------------------------------ inputs
+
+def lcg_rand(n: int, seed: int) -> np.ndarray:
+    """randArr n seed (scripts/AsmTest.lean:7-13): doubles in [-1, 1) from a 64-bit LCG."""
+    out = np.empty(n, dtype=np.float64)
+    x = (seed * 2654435761 + 12345) & 0xFFFFFFFFFFFFFFFF
+    for i in range(n):
+        x = (x * 6364136223846793005 + 1442695040888963407) & 0xFFFFFFFFFFFFFFFF
+        out[i] = ((x >> 11) / 9007199254740992.0) * 2.0 - 1.0
+    return out
+
+
+def uniform_complex(shape, seed: int = 20261016) -> np.ndarray:
+    """re, im iid uniform[-0.5, 0.5) from numpy's default_rng(seed) (the benchmark
+    protocol's seed)."""
+    rng = np.random.default_rng(seed)
+    a = rng.random(tuple(shape) + (2,)) - 0.5
+    return a.view(np.complex128).reshape(shape)
