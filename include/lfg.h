@@ -1,0 +1,110 @@
+/* lfg.h -- C ABI of the GB300 (sm_103a) execute path for lean-fftw problems.
+ *
+ * This library executes lean-fftw's fast-engine transforms on the GPU: 1-D and batched
+ * complex DFTs (binary64 by default) with the reference's own Stockham passes, twiddle
+ * tables and generated butterfly codelets, so a binary64 plan with the same radix sequence
+ * returns bit-identical results.  Problems are described with lean-fftw's FFI encoding.
+ *
+ * Conventions (lean-fftw docs/CONTRACT.md): unnormalised transforms; forward = sign -1;
+ * complex data interleaved (re, im) unless a split layout is given by the spec's offsets.
+ * Every entry point returns an lfg_status; unsupported problems return LFG_ERR_UNSUPPORTED
+ * and never compute a different transform (lean-fftw docs/CONTRACT.md:44-45).
+ */
+#ifndef LFG_H
+#define LFG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  LFG_OK = 0,
+  LFG_ERR_UNSUPPORTED = 1, /* outside the supported problem domain (no plan)          */
+  LFG_ERR_INVALID = 2,     /* malformed arguments (null pointer, bad spec length ...)  */
+  LFG_ERR_CUDA = 3,        /* a CUDA runtime call failed                              */
+  LFG_ERR_NOMEM = 4,       /* host or device allocation failed                        */
+  LFG_ERR_TIMEOUT = 5      /* a bounded device-side wait gave up (ragged work queue)  */
+} lfg_status;
+
+typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
+
+/* Planning flags. */
+#define LFG_ESTIMATE 0u  /* radix sequence with the fewest floating-point operations     */
+#define LFG_MEASURE 1u   /* time the leading candidates on the device, keep the fastest */
+
+typedef struct lfg_plan lfg_plan;
+
+/* Plan a problem given in lean-fftw's FFI encoding (LeanFFTW/FFI.lean:13-21, decoded as in
+ * FFI.lean:32-47): doubles holding small integers
+ *   [kind, sign, rank, vrank, inRe, inIm, outRe, outIm,
+ *    (n, is, os) x rank, (n, is, os) x vrank, r2rkind x rank]
+ * kind 0 = complex DFT, 1 = rdft2 (r2c when sign < 0, c2r otherwise); strides and offsets
+ * are in doubles, relative to the pointers later given to lfg_execute.  Replaces
+ * `lfftw_generic_plan` (LeanFFTW/FFI.lean:50-52) for the kinds and layouts this library
+ * executes.  A vector dimension of size 0 gives an empty plan (Core/Problem.lean:251-256).
+ * Returns LFG_ERR_UNSUPPORTED (and *out = NULL) for anything else. */
+lfg_status lfg_plan_spec(const double *spec, size_t nspec, lfg_precision precision,
+                         unsigned flags, lfg_plan **out);
+
+/* 1-D complex transform of size n, unit stride, interleaved, `howmany` contiguous
+ * transforms (distance n).  sign < 0: forward.  The fast-engine entry point: replaces
+ * `lfa_plan_measure(N, fwd, in, out)` (LeanFFTW/Asm/Planner.lean:293-302), which plans one
+ * transform of a 13-smooth n; this version also batches. */
+lfg_status lfg_plan_1d(size_t n, int sign, size_t howmany, lfg_precision precision,
+                       unsigned flags, lfg_plan **out);
+
+/* As lfg_plan_1d with an explicit radix sequence radices[0..npass) whose product is n
+ * (each radix 2..16): the passes of lean-fftw's `refTransform fwd n radices`
+ * (LeanFFTW/Gen/Stockham.lean:298-301).  Used by the autotuner and by parity tests. */
+lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision precision,
+                               const int *radices, int npass, lfg_plan **out);
+
+/* Execute on device pointers, enqueued on `stream` (a cudaStream_t; NULL = legacy default
+ * stream).  in == out is allowed.  Replaces `lfa_call(rec, in, out)`
+ * (LeanFFTW/Asm/Kernels.lean:1203-1204) and `lfftw_generic_exec` (LeanFFTW/FFI.lean:56-58)
+ * for device-resident data. */
+lfg_status lfg_execute(const lfg_plan *plan, const void *in, void *out, void *stream);
+
+/* Execute on host pointers: copies the spanned input to the device, transforms, copies the
+ * output back, and returns when the output is in `out`.  The host-memory analogue of
+ * `lfa_call` (LeanFFTW/Asm/Kernels.lean:1203-1204) as called by the libbench2 backend
+ * (bench/backends/bench-leanfftw.c:284-288). */
+lfg_status lfg_execute_host(const lfg_plan *plan, const void *in, void *out);
+
+/* Release a plan and its device memory. */
+void lfg_destroy(lfg_plan *plan);
+
+/* Introspection (the analogue of LF_PLAN_SHOW, LeanFFTW/Asm/Planner.lean:299-300):
+ * the radix sequence (up to max_radices entries), number of passes and of kernel groups,
+ * and bytes of input and output per execution. */
+typedef struct {
+  int64_t n;            /* transform size (last dimension)                  */
+  int64_t howmany;      /* number of transforms                              */
+  int sign;
+  int precision;
+  int npass;
+  int ngroups;          /* kernel launches per execution                     */
+  int radices[24];
+  int64_t in_bytes;     /* spanned input bytes per execution                 */
+  int64_t out_bytes;    /* spanned output bytes per execution                */
+  double flops;         /* binary64 instructions of the codelets per execution */
+} lfg_plan_info;
+
+lfg_status lfg_get_plan_info(const lfg_plan *plan, lfg_plan_info *info);
+
+/* Human-readable text of a status, and the last error message of this thread. */
+const char *lfg_strerror(lfg_status s);
+const char *lfg_last_error(void);
+
+/* cos/sin(2*pi*m/n) for m < n as binary64, interleaved, from exact integer arithmetic:
+ * lean-fftw's `Trig.cosSin2PiTable` (LeanFFTW/Core/Trig.lean:131-134). out: 2n doubles. */
+lfg_status lfg_cos_sin_table(uint64_t n, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LFG_H */

@@ -1,0 +1,260 @@
+// C ABI of the GB300 execute path (include/lfg.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/lfg.h"
+#include "kernels.h"
+#include "plan.h"
+#include "trig.h"
+
+struct lfg_plan {
+  lfg::Plan p;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+lfg_status fail(lfg_status s, const std::string& msg) {
+  g_last_error = msg;
+  return s;
+}
+
+lfg_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(LFG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool smooth13(int64_t n) {
+  if (n < 1) return false;
+  for (int p : {2, 3, 5, 7, 11, 13})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+
+int64_t tile_target() {
+  const char* s = std::getenv("LFG_TILE_TARGET");
+  if (s) {
+    long v = std::strtol(s, nullptr, 10);
+    if (v >= 16 && v <= 65536) return v;
+  }
+  return 2048;
+}
+
+// Spanned scalars of a side: from the execution pointer to one past the last element.
+int64_t span_scalars(const lfg::Side& s, int64_t n, int64_t howmany, int per_elem) {
+  return (s.offset + (n - 1) * s.stride + (howmany - 1) * s.dist + 1) * per_elem;
+}
+
+lfg_status finish_c2c(lfg::Plan& p, lfg_plan** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  p.device = dev;
+  if (!p.empty) {
+    e = p.precision == 0 ? lfg::prepare_group_kernels_f64() : cudaErrorNotSupported;
+    if (e != cudaSuccess) return cuda_fail(e, "kernel set-up");
+    std::string msg = lfg::build_c2c(p, tile_target());
+    if (!msg.empty()) {
+      lfg::free_plan_memory(p);
+      return fail(LFG_ERR_UNSUPPORTED, msg);
+    }
+  }
+  p.in_span = span_scalars(p.in, p.n, p.howmany, 2);
+  p.out_span = span_scalars(p.out, p.n, p.howmany, 2);
+  lfg_plan* h = new (std::nothrow) lfg_plan;
+  if (!h) {
+    lfg::free_plan_memory(p);
+    return fail(LFG_ERR_NOMEM, "host allocation");
+  }
+  h->p = p;
+  *out = h;
+  return LFG_OK;
+}
+
+lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision precision,
+                          const int* radices, int npass, lfg_plan** out) {
+  if (!out) return fail(LFG_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (sign != -1 && sign != 1) return fail(LFG_ERR_INVALID, "sign must be -1 or +1");
+  if (precision != LFG_F64) return fail(LFG_ERR_UNSUPPORTED, "precision not supported yet");
+  if (n < 2 || n > ((size_t)1 << 24)) return fail(LFG_ERR_UNSUPPORTED, "size outside 2..2^24");
+  if (!smooth13((int64_t)n)) return fail(LFG_ERR_UNSUPPORTED, "size has a prime factor above 13");
+  lfg::Plan p;
+  p.kind = lfg::Kind::C2C;
+  p.precision = precision;
+  p.fwd = sign < 0;
+  p.n = (int64_t)n;
+  p.howmany = (int64_t)howmany;
+  p.in.stride = p.out.stride = 1;
+  p.in.dist = p.out.dist = (int64_t)n;
+  p.empty = howmany == 0;
+  if (radices) {
+    if (npass < 1 || npass > lfg::kMaxPass) return fail(LFG_ERR_INVALID, "bad pass count");
+    p.radices.assign(radices, radices + npass);
+  } else {
+    p.radices = lfg::choose_radices(p.n, precision);
+  }
+  return finish_c2c(p, out);
+}
+
+}  // namespace
+
+extern "C" {
+
+lfg_status lfg_plan_1d(size_t n, int sign, size_t howmany, lfg_precision precision,
+                       unsigned flags, lfg_plan** out) {
+  (void)flags;
+  return plan_1d_common(n, sign, howmany, precision, nullptr, 0, out);
+}
+
+lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision precision,
+                               const int* radices, int npass, lfg_plan** out) {
+  if (!radices) return fail(LFG_ERR_INVALID, "null radices");
+  return plan_1d_common(n, sign, howmany, precision, radices, npass, out);
+}
+
+// Decode lean-fftw's problem encoding (LeanFFTW/FFI.lean:32-47) and plan the parts this
+// library executes.  Strides and offsets arrive in doubles.
+lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precision,
+                         unsigned flags, lfg_plan** out) {
+  (void)flags;
+  if (!out) return fail(LFG_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!spec || nspec < 8) return fail(LFG_ERR_INVALID, "spec too short");
+  for (size_t i = 0; i < nspec; ++i)
+    if (!std::isfinite(spec[i]) || spec[i] != std::floor(spec[i]))
+      return fail(LFG_ERR_INVALID, "spec entries must be integers");
+  const int kind = (int)spec[0];
+  const int sign = spec[1] < 0 ? -1 : 1;
+  const int64_t rank = (int64_t)spec[2], vrank = (int64_t)spec[3];
+  if (rank < 0 || vrank < 0 || nspec < (size_t)(8 + 3 * (rank + vrank)))
+    return fail(LFG_ERR_INVALID, "spec length does not match rank and vector rank");
+  const int64_t inRe = (int64_t)spec[4], inIm = (int64_t)spec[5];
+  const int64_t outRe = (int64_t)spec[6], outIm = (int64_t)spec[7];
+  auto dim = [&](int64_t i, int64_t* n, int64_t* is, int64_t* os) {
+    *n = (int64_t)spec[8 + 3 * i];
+    *is = (int64_t)spec[9 + 3 * i];
+    *os = (int64_t)spec[10 + 3 * i];
+  };
+  if (precision != LFG_F64) return fail(LFG_ERR_UNSUPPORTED, "precision not supported yet");
+  if (kind != 0) return fail(LFG_ERR_UNSUPPORTED, "only complex DFTs (kind 0) are executed so far");
+  for (int64_t d = 0; d < rank; ++d) {
+    int64_t n, is, os;
+    dim(d, &n, &is, &os);
+    if (n < 1) return fail(LFG_ERR_UNSUPPORTED, "transform dimension must be >= 1");
+  }
+  if (rank != 1) return fail(LFG_ERR_UNSUPPORTED, "only rank-1 transforms are executed so far");
+  if (vrank > 1) return fail(LFG_ERR_UNSUPPORTED, "vector rank > 1 not executed so far");
+  // interleaved complex data: imaginary part one double after the real part, even strides
+  if (inIm != inRe + 1 || outIm != outRe + 1 || inRe < 0 || outRe < 0 || (inRe & 1) || (outRe & 1))
+    return fail(LFG_ERR_UNSUPPORTED, "only interleaved, complex-aligned layouts are executed");
+  int64_t n, is, os;
+  dim(0, &n, &is, &os);
+  int64_t vn = 1, vis = 0, vos = 0;
+  if (vrank == 1) dim(1, &vn, &vis, &vos);
+  if (vn < 0) return fail(LFG_ERR_INVALID, "negative vector dimension");
+  if ((is & 1) || (os & 1) || (vis & 1) || (vos & 1) || is <= 0 || os <= 0 || vis < 0 || vos < 0)
+    return fail(LFG_ERR_UNSUPPORTED, "strides must be positive multiples of a complex element");
+  if (n < 2 || n > ((int64_t)1 << 24) || !smooth13(n))
+    return fail(LFG_ERR_UNSUPPORTED, "size must be 13-smooth in 2..2^24");
+  lfg::Plan p;
+  p.kind = lfg::Kind::C2C;
+  p.precision = precision;
+  p.fwd = sign < 0;
+  p.n = n;
+  p.howmany = vn;
+  p.empty = vn == 0;
+  p.in.offset = inRe / 2;
+  p.in.stride = is / 2;
+  p.in.dist = vrank == 1 ? vis / 2 : 0;
+  p.out.offset = outRe / 2;
+  p.out.stride = os / 2;
+  p.out.dist = vrank == 1 ? vos / 2 : 0;
+  p.radices = lfg::choose_radices(n, precision);
+  return finish_c2c(p, out);
+}
+
+lfg_status lfg_execute(const lfg_plan* plan, const void* in, void* out, void* stream) {
+  if (!plan) return fail(LFG_ERR_INVALID, "null plan");
+  if (plan->p.empty) return LFG_OK;
+  if (!in || !out) return fail(LFG_ERR_INVALID, "null buffer");
+  cudaError_t e = lfg::execute_plan(plan->p, in, out, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "execute");
+  return LFG_OK;
+}
+
+lfg_status lfg_execute_host(const lfg_plan* plan, const void* in, void* out) {
+  if (!plan) return fail(LFG_ERR_INVALID, "null plan");
+  const lfg::Plan& p = plan->p;
+  if (p.empty) return LFG_OK;
+  if (!in || !out) return fail(LFG_ERR_INVALID, "null buffer");
+  const size_t sb = p.precision == 0 ? 8 : 4;
+  const size_t ib = (size_t)p.in_span * sb, ob = (size_t)p.out_span * sb;
+  cudaError_t e;
+  if (!p.d_host_in) {
+    if ((e = cudaMalloc(&p.d_host_in, ib)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    if ((e = cudaMalloc(&p.d_host_out, ob)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  }
+  const bool inplace = in == out;
+  void* din = p.d_host_in;
+  void* dout = inplace ? p.d_host_in : p.d_host_out;
+  if ((e = cudaMemcpy(din, in, ib, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(e, "host-to-device copy");
+  if (!inplace && (e = cudaMemcpy(dout, out, ob, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(e, "host-to-device copy");
+  if ((e = lfg::execute_plan(p, din, dout, 0)) != cudaSuccess) return cuda_fail(e, "execute");
+  if ((e = cudaMemcpy(out, dout, ob, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_fail(e, "device-to-host copy");
+  return LFG_OK;
+}
+
+void lfg_destroy(lfg_plan* plan) {
+  if (!plan) return;
+  lfg::free_plan_memory(plan->p);
+  delete plan;
+}
+
+lfg_status lfg_get_plan_info(const lfg_plan* plan, lfg_plan_info* info) {
+  if (!plan || !info) return fail(LFG_ERR_INVALID, "null argument");
+  const lfg::Plan& p = plan->p;
+  std::memset(info, 0, sizeof *info);
+  info->n = p.n;
+  info->howmany = p.howmany;
+  info->sign = p.fwd ? -1 : 1;
+  info->precision = p.precision;
+  info->npass = (int)p.radices.size();
+  info->ngroups = p.ngroups;
+  for (size_t i = 0; i < p.radices.size() && i < 24; ++i) info->radices[i] = p.radices[i];
+  info->in_bytes = p.in_span * (p.precision == 0 ? 8 : 4);
+  info->out_bytes = p.out_span * (p.precision == 0 ? 8 : 4);
+  info->flops = p.flops;
+  return LFG_OK;
+}
+
+const char* lfg_strerror(lfg_status s) {
+  switch (s) {
+    case LFG_OK: return "ok";
+    case LFG_ERR_UNSUPPORTED: return "problem not supported";
+    case LFG_ERR_INVALID: return "invalid argument";
+    case LFG_ERR_CUDA: return "CUDA error";
+    case LFG_ERR_NOMEM: return "out of memory";
+    case LFG_ERR_TIMEOUT: return "device wait timed out";
+  }
+  return "unknown status";
+}
+
+const char* lfg_last_error(void) { return g_last_error.c_str(); }
+
+lfg_status lfg_cos_sin_table(uint64_t n, double* out) {
+  if (!out || n == 0) return fail(LFG_ERR_INVALID, "bad arguments");
+  std::vector<double> t = lfg::cos_sin_2pi_table(n);
+  std::memcpy(out, t.data(), t.size() * sizeof(double));
+  return LFG_OK;
+}
+
+}  // extern "C"

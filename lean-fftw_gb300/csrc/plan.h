@@ -1,0 +1,62 @@
+// Host-side plan object and planner of the GB300 execute path.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "stockham.h"
+
+namespace lfg {
+
+enum class Kind { C2C, R2C, C2R };
+
+// Layout of one side (input or output) of a batched 1-D transform, in complex (C2C) or real
+// elements of the side's scalar type, relative to the pointer given at execution.
+struct Side {
+  int64_t offset = 0;    // element offset of the first element
+  int64_t stride = 1;    // between consecutive elements of a line
+  int64_t dist = 0;      // between consecutive lines
+};
+
+struct Plan {
+  Kind kind = Kind::C2C;
+  int precision = 0;     // 0: binary64, 1: binary32
+  bool fwd = true;
+  int64_t n = 0;         // transform size
+  int64_t howmany = 1;
+  Side in, out;
+  int64_t in_span = 0;   // spanned input and output, in scalars, from the execution pointer
+  int64_t out_span = 0;
+  std::vector<int> radices;
+  int ngroups = 0;
+  GroupDesc groups[2];
+  int group_first_pass[2] = {0, 0};
+  double flops = 0;      // codelet operations per execution
+  // device memory owned by the plan
+  int device = 0;
+  void* d_twiddles = nullptr;
+  mutable void* d_scratch = nullptr;     // intermediate of in-place two-group transforms
+  mutable size_t scratch_bytes = 0;
+  mutable void* d_host_in = nullptr;     // staging buffers of lfg_execute_host
+  mutable void* d_host_out = nullptr;
+  bool empty = false;    // a vector dimension of size 0: nothing to do
+};
+
+// Radix sequence with the fewest codelet operations for size n (first pass untwiddled),
+// or an empty vector when n is not 13-smooth.
+std::vector<int> choose_radices(int64_t n, int precision);
+
+// Codelet operation count of a plan's radix sequence, per transform.
+double plan_ops(int64_t n, const std::vector<int>& radices);
+
+// Fill groups, tile sizes and twiddle tables of a C2C plan whose size, batch layout and
+// radices are set.  Returns an error message, or "" on success.
+std::string build_c2c(Plan& p, int64_t tile_target);
+
+void free_plan_memory(Plan& p);
+
+cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream);
+
+}  // namespace lfg

@@ -1,0 +1,288 @@
+// Planner of the GB300 execute path: radix choice, pass grouping, twiddle tables.
+//
+// lean-fftw's planner (LeanFFTW/Asm/Planner.lean:84-286) enumerates radix sequences and
+// schedules, prunes them by proved operation counts (`raceOrder`, :196-205) and times the
+// survivors on the CPU.  On GB300 the binary64 path is bound by the FP64 pipe, so the
+// operation count of the codelets is the dominant cost: LFG_ESTIMATE picks the sequence
+// with the fewest codelet operations directly (a dynamic program over the divisors of n),
+// and LFG_MEASURE (api.cpp) times the leading candidates on the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+
+#include "generated/opcounts.h"
+#include "kernels.h"
+#include "plan.h"
+#include "trig.h"
+
+namespace lfg {
+namespace {
+
+bool radix_ok(int R) { return R >= 2 && R <= kMaxRadix && kOpsUntw[R] > 0; }
+
+// per-point operations of a twiddled pass of radix R
+double tw_cost(int R) { return (double)kOpsTw[R] / R; }
+double untw_cost(int R) { return (double)kOpsUntw[R] / R; }
+
+struct Best {
+  double cost;
+  std::vector<int> seq;
+};
+
+// Cheapest sequence of twiddled radices with product m (per point), memoised.
+const Best& best_tail(int64_t m, std::map<int64_t, Best>& memo) {
+  auto it = memo.find(m);
+  if (it != memo.end()) return it->second;
+  Best b{INFINITY, {}};
+  if (m == 1) {
+    b.cost = 0;
+  } else {
+    for (int R = kMaxRadix; R >= 2; --R) {
+      if (!radix_ok(R) || m % R) continue;
+      const Best& t = best_tail(m / R, memo);
+      if (!std::isfinite(t.cost)) continue;
+      double c = tw_cost(R) + t.cost;
+      // fewer operations first; on a tie, fewer passes
+      if (c < b.cost - 1e-12 || (std::fabs(c - b.cost) <= 1e-12 && t.seq.size() + 1 < b.seq.size())) {
+        b.cost = c;
+        b.seq = t.seq;
+        b.seq.insert(b.seq.begin(), R);
+      }
+    }
+  }
+  return memo[m] = b;
+}
+
+// Largest divisor of n that is <= cap (at least 1).
+int64_t divisor_at_most(int64_t n, int64_t cap) {
+  if (cap >= n) return n;
+  for (int64_t d = cap; d >= 1; --d)
+    if (n % d == 0) return d;
+  return 1;
+}
+
+size_t smem_bytes(int64_t C, int64_t M, int precision) {
+  return 2 * (size_t)C * (size_t)M * (precision == 0 ? 16 : 8);
+}
+
+}  // namespace
+
+std::vector<int> choose_radices(int64_t n, int precision) {
+  (void)precision;
+  if (n < 2) return {};
+  std::map<int64_t, Best> memo;
+  double best = INFINITY;
+  std::vector<int> seq;
+  for (int R0 = kMaxRadix; R0 >= 2; --R0) {
+    if (!radix_ok(R0) || n % R0) continue;
+    const Best& t = best_tail(n / R0, memo);
+    if (!std::isfinite(t.cost)) continue;
+    double c = untw_cost(R0) + t.cost;
+    if (c < best - 1e-12 || (std::fabs(c - best) <= 1e-12 && t.seq.size() + 1 < seq.size())) {
+      best = c;
+      seq = t.seq;
+      seq.insert(seq.begin(), R0);
+    }
+  }
+  return seq;
+}
+
+double plan_ops(int64_t n, const std::vector<int>& rs) {
+  double ops = 0;
+  for (size_t t = 0; t < rs.size(); ++t)
+    ops += (double)(n / rs[t]) * (t == 0 ? kOpsUntw[rs[t]] : kOpsTw[rs[t]]);
+  return ops;
+}
+
+void free_plan_memory(Plan& p) {
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != p.device) cudaSetDevice(p.device);
+  if (p.d_twiddles) cudaFree(p.d_twiddles);
+  if (p.d_scratch) cudaFree(p.d_scratch);
+  if (p.d_host_in) cudaFree(p.d_host_in);
+  if (p.d_host_out) cudaFree(p.d_host_out);
+  p.d_twiddles = p.d_scratch = p.d_host_in = p.d_host_out = nullptr;
+  if (cur != p.device) cudaSetDevice(cur);
+}
+
+std::string build_c2c(Plan& p, int64_t tile_target) {
+  const int64_t N = p.n;
+  const int prec = p.precision;
+  const size_t elem = prec == 0 ? 16 : 8;
+  const int64_t max_single = (int64_t)(kMaxSmemBytes / (2 * elem));
+  std::vector<int>& rs = p.radices;
+  if (rs.empty()) return "no radix sequence";
+  if ((int)rs.size() > kMaxPass) return "too many passes";
+  int64_t prod = 1;
+  for (int R : rs) {
+    if (!radix_ok(R)) return "radix " + std::to_string(R) + " has no codelet";
+    prod *= R;
+  }
+  if (prod != N) return "radices do not multiply to n";
+
+  // pass grouping: one group when a transform fits one CTA's shared memory, else split the
+  // sequence after the prefix whose product P best balances P against N/P
+  int split = (int)rs.size();
+  if (N > max_single) {
+    int best = -1;
+    int64_t bestv = INT64_MAX;
+    int64_t P = 1;
+    for (int t = 0; t + 1 < (int)rs.size(); ++t) {
+      P *= rs[t];
+      int64_t Q = N / P;
+      if (P > max_single || Q > max_single) continue;
+      int64_t v = std::max(P, Q);
+      if (v < bestv) { bestv = v; best = t + 1; }
+    }
+    if (best < 0) return "size too large for two pass groups with this radix order";
+    split = best;
+  }
+
+  // twiddle tables of every pass t >= 1, concatenated (each 16-byte aligned)
+  std::vector<double> tab = cos_sin_2pi_table((uint64_t)N);
+  std::vector<size_t> toff(rs.size(), 0);
+  size_t total = 0;
+  std::vector<int64_t> ns(rs.size());
+  int64_t acc = 1;
+  for (size_t t = 0; t < rs.size(); ++t) {
+    ns[t] = acc;
+    acc *= rs[t];
+    if (t == 0) continue;
+    toff[t] = total;
+    total += 2 * (size_t)(rs[t] - 1) * ns[t];
+    total = (total + 1) & ~(size_t)1;
+  }
+  std::vector<double> host(std::max<size_t>(total, 2));
+  for (size_t t = 1; t < rs.size(); ++t)
+    pass_twiddles(tab, p.fwd, (uint64_t)N, rs[t], (uint64_t)ns[t], host.data() + toff[t]);
+  size_t tw_bytes;
+  std::vector<float> host32;
+  if (prec == 0) {
+    tw_bytes = host.size() * sizeof(double);
+  } else {
+    host32.assign(host.begin(), host.end());
+    tw_bytes = host32.size() * sizeof(float);
+  }
+  if (cudaMalloc(&p.d_twiddles, tw_bytes) != cudaSuccess) return "cudaMalloc of twiddle tables failed";
+  cudaError_t e = cudaMemcpy(p.d_twiddles, prec == 0 ? (const void*)host.data() : (const void*)host32.data(),
+                             tw_bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return std::string("twiddle upload: ") + cudaGetErrorString(e);
+  auto tw_ptr = [&](size_t t) -> const void* {
+    if (t == 0) return nullptr;
+    return prec == 0 ? (const void*)((const double*)p.d_twiddles + toff[t])
+                     : (const void*)((const float*)p.d_twiddles + toff[t]);
+  };
+
+  auto make_group = [&](GroupDesc& g, int t0, int t1, int64_t nsub, int64_t nsub_div_hint) {
+    int64_t M = 1;
+    for (int t = t0; t < t1; ++t) M *= rs[t];
+    g.M = (int)M;
+    g.npass = t1 - t0;
+    g.nsub = (int)nsub;
+    int64_t cmax = std::max<int64_t>(1, tile_target / M);
+    while (cmax > 1 && smem_bytes(cmax, M, prec) > kMaxSmemBytes) --cmax;
+    g.C = (int)divisor_at_most(nsub_div_hint, cmax);
+    int64_t P0 = 1;
+    for (int t = 0; t < t0; ++t) P0 *= rs[t];
+    g.kmul = (int)P0;
+    g.twsub = t0 > 0 ? 1 : 0;
+    for (int t = t0; t < t1; ++t) {
+      PassDesc& d = g.pass[t - t0];
+      d.R = rs[t];
+      d.ns_g = (int)ns[t];
+      d.ns_loc = (int)(ns[t] / P0);
+      d.tw = tw_ptr(t);
+    }
+  };
+
+  p.flops = plan_ops(N, rs) * (double)p.howmany;
+  if (split == (int)rs.size()) {
+    p.ngroups = 1;
+    GroupDesc& g = p.groups[0];
+    // lines may share a tile; pick C by the target only (the batch need not divide)
+    make_group(g, 0, (int)rs.size(), 1, 1);
+    int64_t cmax = std::max<int64_t>(1, tile_target / N);
+    while (cmax > 1 && smem_bytes(cmax, N, prec) > kMaxSmemBytes) --cmax;
+    g.C = (int)std::min<int64_t>(cmax, std::max<int64_t>(1, p.howmany));
+    g.total_sub = p.howmany;
+    g.in_line = p.in.dist;
+    g.in_sub = 0;
+    g.in_elem = p.in.stride;
+    g.out_line = p.out.dist;
+    g.out_sub = 0;
+    g.out_elem = p.out.stride;
+    p.group_first_pass[0] = 0;
+  } else {
+    p.ngroups = 2;
+    int64_t P = 1;
+    for (int t = 0; t < split; ++t) P *= rs[t];
+    const int64_t Q = N / P;
+    GroupDesc& g1 = p.groups[0];
+    GroupDesc& g2 = p.groups[1];
+    make_group(g1, 0, split, Q, Q);
+    make_group(g2, split, (int)rs.size(), P, P);
+    g1.total_sub = p.howmany * Q;
+    g2.total_sub = p.howmany * P;
+    // group 1: sub-problem b reads x[b + Q*i], writes z[b*P + m]; the intermediate z
+    // layout (line, stride) is filled in at execution (out, or the scratch buffer)
+    g1.in_line = p.in.dist;
+    g1.in_sub = p.in.stride;
+    g1.in_elem = Q * p.in.stride;
+    // group 2: sub-problem m reads z[i*P + m] and writes out[o*P + m]
+    g2.out_line = p.out.dist;
+    g2.out_sub = p.out.stride;
+    g2.out_elem = P * p.out.stride;
+    p.group_first_pass[0] = 0;
+    p.group_first_pass[1] = split;
+  }
+  return "";
+}
+
+cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream) {
+  if (p.empty) return cudaSuccess;
+  const size_t es = p.precision == 0 ? 16 : 8;
+  const char* ib = static_cast<const char*>(in) + p.in.offset * (int64_t)es;
+  char* ob = static_cast<char*>(out) + p.out.offset * (int64_t)es;
+  auto launch = [&](const GroupDesc& g, const void* a, void* b) -> cudaError_t {
+    if (p.precision == 0) return launch_group_f64(g, p.fwd, a, b, stream);
+    return cudaErrorNotSupported;
+  };
+  if (p.ngroups == 1) return launch(p.groups[0], ib, ob);
+  // two groups: the intermediate goes to `out` when it does not alias the input, else to the
+  // plan's scratch buffer (allocated on first use)
+  GroupDesc g1 = p.groups[0], g2 = p.groups[1];
+  const int64_t P = g2.nsub;
+  char* zb;
+  int64_t z_line, z_stride;
+  if (in != out) {
+    zb = ob;
+    z_line = p.out.dist;
+    z_stride = p.out.stride;
+  } else {
+    size_t need = (size_t)p.n * (size_t)p.howmany * es;
+    if (p.scratch_bytes < need) {
+      if (p.d_scratch) cudaFree(p.d_scratch);
+      p.d_scratch = nullptr;
+      p.scratch_bytes = 0;
+      cudaError_t e = cudaMalloc(&p.d_scratch, need);
+      if (e != cudaSuccess) return e;
+      p.scratch_bytes = need;
+    }
+    zb = static_cast<char*>(p.d_scratch);
+    z_line = p.n;
+    z_stride = 1;
+  }
+  g1.out_line = z_line;
+  g1.out_sub = P * z_stride;
+  g1.out_elem = z_stride;
+  g2.in_line = z_line;
+  g2.in_sub = z_stride;
+  g2.in_elem = P * z_stride;
+  cudaError_t e = launch(g1, ib, zb);
+  if (e != cudaSuccess) return e;
+  return launch(g2, zb, ob);
+}
+
+}  // namespace lfg

@@ -1,0 +1,57 @@
+// Descriptors shared by the host planner and the Stockham group kernels.
+//
+// A transform of size N = R_0 ... R_{s-1} runs s Stockham passes (lean-fftw
+// `LeanFFTW/Gen/Stockham.lean:276-294`): pass t has ns = R_0 ... R_{t-1}; butterfly
+// j = b*ns + k reads z[j + r*N/R], multiplies input r >= 1 by the table twiddle w_r(k) when
+// t >= 1, and writes output r to position b*ns*R + k + r*ns.
+//
+// The GPU runs the passes in one or more *groups*.  A group is a run of consecutive passes
+// whose data dependencies close over independent sub-problems of length M (the product of
+// the group's radices), so one CTA can load a tile of sub-problems into shared memory, run
+// every pass of the group there, and store the tile back:
+//
+//   * one group (N fits in shared memory): sub-problem = one whole transform;
+//   * first of two groups (passes 0..T-1, product P): sub-problem b < N/P is the
+//     stride-N/P subsequence x[b + (N/P) i], written contiguously to z[b*P + m];
+//   * second group (passes T..s-1): sub-problem m < P is the stride-P subsequence
+//     z[q*P + m]; it is read and written in place, and the table index of a twiddle is
+//     k = k_local*P + m.
+//
+// Both facts follow from the pass formula: after passes 0..T-1, positions b*P..b*P+P-1 hold
+// the size-P transform of x[b + (N/P) i]; every later pass maps positions = m (mod P) to
+// positions = m (mod P), since N/R and ns are multiples of P.  Each butterfly therefore
+// performs exactly the operations of the reference pass, so the result is bit-identical to
+// the reference transform for the same radix sequence.
+#pragma once
+#include <cstdint>
+
+namespace lfg {
+
+constexpr int kMaxPass = 24;       // lean-fftw Asm/Planner.lean:49 (`maxPass`)
+constexpr int kMaxRadix = 16;
+
+struct PassDesc {
+  int R;                 // radix of the pass
+  int ns_loc;            // product of the group's earlier radices
+  int ns_g;              // product of all earlier radices of the transform (table row length)
+  int pad_;
+  const void* tw;        // pass twiddle table (2*(R-1)*ns_g scalars), nullptr for pass 0
+};
+
+// Complex element (s, i) of sub-problem s (flattened over lines) lives at
+//   base + (s / nsub) * line_stride + (s % nsub) * sub_stride + i * elem_stride
+// in units of complex elements, separately for input and output.
+struct GroupDesc {
+  int M;                 // sub-problem length
+  int npass;
+  int nsub;              // sub-problems per line
+  int C;                 // sub-problems per CTA tile
+  int64_t total_sub;     // lines * nsub
+  int64_t in_line, in_sub, in_elem;
+  int64_t out_line, out_sub, out_elem;
+  int kmul;              // table index k = k_loc * kmul + (twsub ? s % nsub : 0)
+  int twsub;
+  PassDesc pass[kMaxPass];
+};
+
+}  // namespace lfg

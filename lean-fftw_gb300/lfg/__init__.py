@@ -1,0 +1,12 @@
+"""lfg: GB300-native execute path for lean-fftw's 1-D and batched transforms.
+
+The transforms run in hand-written sm_103a CUDA kernels inside lfg/liblfg.so (C ABI:
+include/lfg.h); this package holds the Python mirror of lean-fftw's plan/execute
+interface (`plan`), the torch integration and the codelet generator used at build time
+(`codegen`).
+"""
+from ._lib import LfgError, Unsupported, lib  # noqa: F401
+from .plan import Plan, cos_sin_table, plan_1d, plan_measure, plan_spec  # noqa: F401
+
+__all__ = ["Plan", "plan_1d", "plan_measure", "plan_spec", "cos_sin_table", "LfgError",
+           "Unsupported", "lib"]
