@@ -4,14 +4,20 @@
 
 Workloads (synthetic inputs, re/im iid uniform[-0.5, 0.5) from numpy default_rng(20261016)):
 
-  c2c_1024   1-D complex FP64 forward, N = 1024, batch 65536 (1 GiB in, 1 GiB out); the
-             power-of-two sweep's shape at N = 1024 (batch = 2^26 / N).
+  ragged     (default, the headline) 8192 1-D complex FP64 forward transforms, sizes drawn
+             log-uniformly from [2, 16384] and snapped to the nearest 13-smooth integer in
+             log distance (859 distinct sizes, sum 14,922,904 points), packed back to back
+             in size order; one persistent launch replayed from a CUDA graph.  The same batch
+             with one launch per distinct size is timed beside it (`per_size`).
+  c2c_<N>    1-D complex FP64 forward, N = 2^k (k = 1..18), batch 2^26 / N (1 GiB in and
+             out): the power-of-two sweep.
 
-A step is one execution of the plan over the whole batch.  `value` is GFLOP/s with the
-conventional 5 N log2 N flops per transform, inputs resident in HBM; `e2e` is the same
-metric through the C ABI's host-pointer entry point (lfg_execute_host), host-to-device and
-device-to-host copies inside the timed region.  Inputs are larger than L2 (129 MB), so no
-L2 flush is needed between steps.
+A step is one execution over the whole batch.  `value` is GFLOP/s with the conventional
+5 N log2 N flops per transform, inputs resident in HBM; `e2e` is the same metric through
+the C ABI's host-pointer entry points (lfg_execute_host / lfg_execute_ragged_host),
+host-to-device and device-to-host copies inside the timed region.  The ragged batch moves
+239 MB in and out per step and the sweep 2 GiB, both above the 129 MB L2, so no L2 flush
+is needed between steps.
 
 `--impl reference` times lean-fftw's reference algorithm on the host cores instead: the
 oracle's C restatement of refTransform with the reference's codelets (the reference engine
@@ -36,9 +42,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "lean-fftw_gb300"))
 
 SEED = 20261016
-WORKLOADS = {
-    "c2c_1024": dict(kind="c2c", n=1024, batch=65536, sign=-1),
-}
+WORKLOADS = {"ragged": dict(kind="ragged", count=8192, sign=-1)}
+for _k in range(1, 19):
+    WORKLOADS[f"c2c_{1 << _k}"] = dict(kind="c2c", n=1 << _k, batch=(1 << 26) >> _k, sign=-1)
 
 
 def peaks():
@@ -134,31 +140,51 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_reference(wl, steps, warmup, sample_transforms=None, budget_s=None):
-    """Time the oracle's restatement of refTransform on all host threads."""
+def cpu_reference(wl, steps, warmup, budget_s=None):
+    """Time the oracle's restatement of refTransform on all host threads (one transform per
+    thread) on a bounded sample of the workload; returns (GFLOP/s, threads, sample text)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as O
     threads = os.cpu_count() or 1
-    n = wl["n"]
-    rs = reference_plan(n)
-    if sample_transforms is None:
-        sample_transforms = max(threads, min(wl["batch"], threads * max(1, (1 << 14) // n)))
-    x = O.uniform_complex((sample_transforms, n), seed=SEED)
-    O.ref_transform(wl["sign"] < 0, n, rs, x[:threads], nthreads=threads)  # warm caches/tables
-    times = []
+    if wl["kind"] == "ragged":
+        sizes = ragged_workload_sizes(wl)
+        plans = {int(n): reference_plan(int(n)) for n in set(sizes.tolist())}
+        off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+        runner = O.RaggedRef(wl["sign"] < 0, sizes, plans, off, off)
+        x = O.uniform_complex((int(sizes.sum()),), seed=SEED)
+        y = np.empty_like(x)
+        call = lambda: runner.run(x, y, nthreads=threads)
+        flops = float(sum(flops_per_transform(int(n)) for n in sizes))
+        sample = f"the whole batch ({len(sizes)} transforms, {len(plans)} sizes) per timed call"
+    else:
+        n = wl["n"]
+        rs = reference_plan(n)
+        count = max(threads, min(wl["batch"], threads * max(1, (1 << 15) // n)))
+        x = O.uniform_complex((count, n), seed=SEED)
+        call = lambda: O.ref_transform(wl["sign"] < 0, n, rs, x, nthreads=threads)
+        flops = flops_per_transform(n) * count
+        sample = f"{count} of the {wl['batch']} transforms of N={n} (plan {'x'.join(map(str, rs))}) per timed call"
+    call()
     for _ in range(warmup):
-        O.ref_transform(wl["sign"] < 0, n, rs, x, nthreads=threads)
-    for _ in range(steps):
+        call()
+    times = []
+    for _ in range(max(1, steps)):
         t0 = time.perf_counter()
-        O.ref_transform(wl["sign"] < 0, n, rs, x, nthreads=threads)
+        call()
         times.append(time.perf_counter() - t0)
         if budget_s and sum(times) > budget_s:
             break
     t = statistics.median(times)
-    gflops = flops_per_transform(n) * sample_transforms / t / 1e9
-    return gflops, threads, f"{sample_transforms} transforms of N={n} (plan {'x'.join(map(str, rs))}) " \
-                            f"per timed call, median of {len(times)}"
+    return flops / t / 1e9, threads, sample + f", median of {len(times)}"
+
+
+def ragged_workload_sizes(wl):
+    """The benchmark's ragged sizes, in increasing order (so that the per-size strategy can
+    run one batched launch per distinct size)."""
+    import numpy as np
+    from lfg.ragged import ragged_sizes
+    return np.sort(ragged_sizes(wl["count"], SEED), kind="stable")
 
 
 def reference_plan(n):
@@ -172,18 +198,27 @@ def reference_plan(n):
     return choose_radices(n)
 
 
+METRIC = "FP64 c2c FFT GFLOP/s (5 N log2 N)"
+
+
+def workload_config(name, wl):
+    if wl["kind"] == "ragged":
+        return {"workload": name, "transforms": wl["count"], "sizes": "13-smooth in [2, 16384], "
+                "log-uniform, seed 20261016", "sign": wl["sign"], "layout": "packed, size order"}
+    return {"workload": name, "n": wl["n"], "batch": wl["batch"], "sign": wl["sign"]}
+
+
 def run_reference(args, wl):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     gf, threads, sample = cpu_reference(wl, max(1, args.steps), max(0, min(args.warmup, 2)),
                                         budget_s=60)
-    line = {"metric": "FP64 c2c FFT GFLOP/s (5 N log2 N)", "value": round(gf, 3),
+    line = {"metric": METRIC, "value": round(gf, 3),
             "unit": "GFLOP/s", "impl": "reference", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "n": wl["n"], "batch": wl["batch"],
-                       "sign": wl["sign"]},
+            "config": workload_config(args.workload, wl),
             "cpu_baseline": {"value": round(gf, 3), "unit": "GFLOP/s", "cores": threads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": round(gf, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
@@ -191,12 +226,28 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def timed(step, steps, stream, local, barrier):
+    """K steps bracketed by a barrier and a synchronize, CUDA events on `stream`."""
+    import torch
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    return ev0.elapsed_time(ev1) / steps, clk.summary()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="c2c_1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="ragged", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="lfg", choices=["lfg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -211,111 +262,134 @@ def main():
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    dist = None
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
     def barrier():
-        if ws > 1:
-            import torch.distributed as dist
+        if dist is not None:
             dist.barrier()
 
-    n, B, sign = wl["n"], wl["batch"], wl["sign"]
-    plan = lfg.plan_1d(n, sign, B)
-    info = plan.info()
+    def max_over_ranks(v):
+        if dist is None:
+            return v
+        t = torch.tensor([v], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    stream = torch.cuda.current_stream()
     rng = np.random.default_rng(SEED + rank)
-    host = (rng.random((B, n, 2)) - 0.5).view(np.complex128).reshape(B, n)
+    extra = {}
+    if wl["kind"] == "ragged":
+        sizes = ragged_workload_sizes(wl)
+        total = int(sizes.sum())
+        plan = lfg.plan_ragged(sizes, wl["sign"])
+        per_size = lfg.plan_ragged(sizes, wl["sign"], per_size=True)
+        rinfo = plan.info()
+        host = (rng.random((total, 2)) - 0.5).view(np.complex128).reshape(total)
+        flops_step = float(sum(flops_per_transform(int(n)) for n in sizes))
+        points = total
+        launches_per_step = int(rinfo.launches)
+        codelet_ops = rinfo.flops
+        step_fn = lambda: plan.execute(x, y)
+        host_fn = lambda a, b: plan.execute_host(a, b)
+        extra["config_extra"] = {"distinct_sizes": int(rinfo.classes), "points": total,
+                                 "work_items": int(rinfo.items), "grid": int(rinfo.grid),
+                                 "smem_bytes": int(rinfo.smem_bytes)}
+    else:
+        n, B = wl["n"], wl["batch"]
+        plan = lfg.plan_1d(n, wl["sign"], B)
+        info = plan.info()
+        host = (rng.random((B, n, 2)) - 0.5).view(np.complex128).reshape(B, n)
+        flops_step = flops_per_transform(n) * B
+        points = n * B
+        launches_per_step = int(info.ngroups)
+        codelet_ops = info.flops
+        step_fn = lambda: plan.execute(x, y)
+        host_fn = lambda a, b: plan.execute_host(a, b)
+        extra["config_extra"] = {"radices": [info.radices[i] for i in range(info.npass)]}
     x = torch.from_numpy(host).to(dev)
     y = torch.empty_like(x)
-    stream = torch.cuda.current_stream()
-
     for _ in range(max(3, args.warmup)):
-        plan.execute(x, y)
+        step_fn()
     torch.cuda.synchronize()
 
-    # headline: K steps, device-resident inputs, CUDA events on the launching stream
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    torch.cuda.synchronize()
-    with Clocks(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            plan.execute(x, y)
-        ev1.record(stream)
+    # headline: device-resident inputs
+    ms, clocks = timed(step_fn, args.steps, stream, local, barrier)
+    ms = max_over_ranks(ms)
+    value = flops_step * ws / (ms * 1e-3) / 1e9
+
+    if wl["kind"] == "ragged":
+        y2 = torch.empty_like(x)
+        ps_step = lambda: per_size.execute(x, y2)
+        for _ in range(3):
+            ps_step()
+        ps_ms, _ = timed(ps_step, max(5, args.steps // 4), stream, local, barrier)
+        ps_ms = max_over_ranks(ps_ms)
         torch.cuda.synchronize()
-    barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    total_flops = flops_per_transform(n) * B * ws
-    value = total_flops / (ms * 1e-3) / 1e9
+        extra["per_size"] = {"value": round(flops_step * ws / (ps_ms * 1e-3) / 1e9, 3),
+                             "unit": "GFLOP/s", "ms_per_step": round(ps_ms, 4),
+                             "launches_per_step": int(per_size.info().launches),
+                             "speedup_of_persistent": round(ps_ms / ms, 3),
+                             "same_bits": bool(torch.equal(y.view(torch.float64),
+                                                           y2.view(torch.float64)))}
 
-    # dominant kernel: per-launch duration of each group, events around each launch
-    group_ms = []
-    if info.ngroups == 1:
-        group_ms = [ms]
-    kernel_ms = ms / info.ngroups if info.ngroups > 1 else ms
-    alg_bytes = 32.0 * n * B            # read + write of the data, one pass over HBM
+    # roofline of the dominant kernel (one launch per step for ragged and single-group sizes)
+    alg_bytes = 32.0 * points            # read + write of the data once
     hbm_peak, peak_kind = peaks()
-    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9 if info.ngroups == 1 else \
-        alg_bytes * info.ngroups / (ms * 1e-3) / 1e9
-    traffic = ncu_traffic(args.workload)
+    kernel_ms = ms / launches_per_step
+    achieved = alg_bytes / launches_per_step / (kernel_ms * 1e-3) / 1e9
     fp64p = fp64_peak()
-    fp64_ach = info.flops / (ms * 1e-3) / 1e12
+    fp64_ach = codelet_ops / (ms * 1e-3) / 1e12
 
     # end to end through the C ABI's host-pointer entry point (pinned host buffers)
     hin = torch.from_numpy(host).pin_memory()
     hout = torch.empty_like(hin).pin_memory()
     hin_np, hout_np = hin.numpy(), hout.numpy()
-    plan.execute_host(hin_np, hout_np)
-    e2e_steps = max(2, min(args.steps, 5))
+    host_fn(hin_np, hout_np)
+    e2e_steps = max(2, min(args.steps, 10))
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        plan.execute_host(hin_np, hout_np)
-    t_e2e = (time.perf_counter() - t0) / e2e_steps
-    if ws > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = total_flops / t_e2e / 1e9
+        host_fn(hin_np, hout_np)
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / e2e_steps)
+    e2e = flops_step * ws / t_e2e / 1e9
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        gf, threads, sample = cpu_reference(wl, 3, 1, budget_s=20)
+        gf, threads, sample = cpu_reference(wl, 5, 1, budget_s=20)
         cpu = {"value": round(gf, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
                "sample": sample}
 
     if rank == 0:
+        config = workload_config(args.workload, wl)
+        config.update(extra.pop("config_extra"))
+        config["l2_flush"] = "inputs larger than L2 (129 MB)"
+        config["parallelism"] = f"replicas{ws}"
         line = {
-            "metric": "FP64 c2c FFT GFLOP/s (5 N log2 N)", "value": round(value, 3),
-            "unit": "GFLOP/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "n": n, "batch": B, "sign": sign,
-                       "radices": [info.radices[i] for i in range(info.npass)],
-                       "l2_flush": "inputs (1 GiB) larger than L2", "parallelism": f"replicas{ws}"},
+            "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-                         "peak_kind": peak_kind,
-                         "traffic": traffic},
+                         "peak_kind": peak_kind, "traffic": ncu_traffic(args.workload),
+                         "algorithmic_bytes_per_launch": alg_bytes / launches_per_step},
             "fp64_issue": {"achieved": round(fp64_ach, 4), "unit": "T FP64 instr/s",
                            "peak": fp64p, "frac": round(fp64_ach / fp64p, 4) if fp64p else None,
                            "note": "codelet binary64 instructions per step / step time; peak = "
-                                   "measured DFMA issue rate"},
+                                   "measured DFMA issue rate (DADD/DMUL issue at 0.505)"},
             "e2e": {"value": round(e2e, 3), "unit": "GFLOP/s",
                     "h2d_bytes_per_step": int(hin.numel() * 16),
                     "d2h_bytes_per_step": int(hout.numel() * 16)},
-            "gpu_launches": int(info.ngroups * args.steps),
+            "gpu_launches": int(launches_per_step * args.steps),
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "clocks": clocks,
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
-    if ws > 1:
-        import torch.distributed as dist
+    if dist is not None:
         dist.destroy_process_group()
 
 

@@ -32,8 +32,10 @@ typedef enum {
 typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
 
 /* Planning flags. */
-#define LFG_ESTIMATE 0u  /* radix sequence with the fewest floating-point operations     */
-#define LFG_MEASURE 1u   /* time the leading candidates on the device, keep the fastest */
+#define LFG_ESTIMATE 0u      /* radix sequence with the fewest floating-point operations     */
+#define LFG_MEASURE 1u       /* time the leading candidates on the device, keep the fastest */
+#define LFG_PER_SIZE 2u      /* ragged: one launch per distinct size (the comparison point)  */
+#define LFG_NO_GRAPH 4u      /* ragged: launch directly instead of replaying a CUDA graph    */
 
 typedef struct lfg_plan lfg_plan;
 
@@ -94,6 +96,54 @@ typedef struct {
 } lfg_plan_info;
 
 lfg_status lfg_get_plan_info(const lfg_plan *plan, lfg_plan_info *info);
+
+/* ---- Ragged batches: many transforms of different sizes in one persistent launch ----
+ *
+ * `count` 1-D complex transforms, transform i of size sizes[i] (13-smooth, 2..2^24), unit
+ * stride, its data starting at complex element in_offsets[i] / out_offsets[i] of the
+ * buffers given at execution (NULL offsets: packed back to back in the given order).
+ * Out of place only; outputs must not overlap.  lean-fftw plans and runs one size at a
+ * time (bench/backends/bench-leanfftw.c:270-291, LeanFFTW/Asm/Planner.lean:224-286); this
+ * plans the whole batch once and executes it as one CUDA-graph-replayed persistent kernel.
+ * Each output is bit-identical to lean-fftw's refTransform for its size and the radix
+ * sequence the plan picked (lfg_get_ragged_radices). */
+typedef struct lfg_ragged lfg_ragged;
+
+/* Autotuning knobs (NULL = defaults): complex elements per CTA tile, largest size run as a
+ * single shared-memory pass group, and per-size radix overrides (n_over entries; entry j is
+ * size over_n[j] with over_radices[24*j .. 24*j + over_npass[j])). */
+typedef struct {
+  int64_t tile_target;
+  int64_t single_max;
+  int n_over;
+  const int64_t *over_n;
+  const int *over_npass;
+  const int *over_radices;
+} lfg_ragged_tuning;
+
+lfg_status lfg_plan_ragged(const int64_t *sizes, size_t count, const int64_t *in_offsets,
+                           const int64_t *out_offsets, int sign, lfg_precision precision,
+                           unsigned flags, const lfg_ragged_tuning *tuning, lfg_ragged **out);
+lfg_status lfg_execute_ragged(const lfg_ragged *plan, const void *in, void *out, void *stream);
+/* Host buffers: copies the spanned input in, executes, copies the spanned output back. */
+lfg_status lfg_execute_ragged_host(const lfg_ragged *plan, const void *in, void *out);
+void lfg_destroy_ragged(lfg_ragged *plan);
+
+typedef struct {
+  int64_t count;        /* transforms                                    */
+  int64_t classes;      /* distinct sizes                                */
+  int64_t items;        /* work items of the persistent kernel           */
+  int64_t grid;         /* CTAs of the persistent kernel                 */
+  int64_t smem_bytes;   /* shared memory per CTA                         */
+  int64_t launches;     /* kernel launches per execution                 */
+  int64_t in_bytes, out_bytes;
+  int64_t points;       /* sum of the sizes                              */
+  double flops;         /* binary64 instructions of the codelets         */
+} lfg_ragged_info;
+
+lfg_status lfg_get_ragged_info(const lfg_ragged *plan, lfg_ragged_info *info);
+/* Radix sequence used for size n (npass = 0 if n is not in the batch). */
+lfg_status lfg_get_ragged_radices(const lfg_ragged *plan, int64_t n, int *radices, int *npass);
 
 /* Human-readable text of a status, and the last error message of this thread. */
 const char *lfg_strerror(lfg_status s);

@@ -1,6 +1,7 @@
 // C ABI of the GB300 execute path (include/lfg.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -10,10 +11,15 @@
 #include "../../include/lfg.h"
 #include "kernels.h"
 #include "plan.h"
+#include "ragged.h"
 #include "trig.h"
 
 struct lfg_plan {
   lfg::Plan p;
+};
+
+struct lfg_ragged {
+  lfg::RaggedPlan r;
 };
 
 namespace {
@@ -233,6 +239,147 @@ lfg_status lfg_get_plan_info(const lfg_plan* plan, lfg_plan_info* info) {
   info->in_bytes = p.in_span * (p.precision == 0 ? 8 : 4);
   info->out_bytes = p.out_span * (p.precision == 0 ? 8 : 4);
   info->flops = p.flops;
+  return LFG_OK;
+}
+
+lfg_status lfg_plan_ragged(const int64_t* sizes, size_t count, const int64_t* in_offsets,
+                           const int64_t* out_offsets, int sign, lfg_precision precision,
+                           unsigned flags, const lfg_ragged_tuning* tuning, lfg_ragged** out) {
+  if (!out) return fail(LFG_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!sizes && count) return fail(LFG_ERR_INVALID, "null sizes");
+  if (sign != -1 && sign != 1) return fail(LFG_ERR_INVALID, "sign must be -1 or +1");
+  if (precision != LFG_F64) return fail(LFG_ERR_UNSUPPORTED, "precision not supported yet");
+  lfg::RaggedPlan r;
+  r.precision = precision;
+  r.fwd = sign < 0;
+  r.empty = count == 0;
+  r.use_graph = !(flags & LFG_NO_GRAPH);
+  r.per_size_mode = (flags & LFG_PER_SIZE) != 0;
+  r.sizes.assign(sizes, sizes + count);
+  int64_t acc_in = 0, acc_out = 0;
+  for (size_t i = 0; i < count; ++i) {
+    const int64_t n = sizes[i];
+    if (n < 2 || n > ((int64_t)1 << 24) || !smooth13(n))
+      return fail(LFG_ERR_UNSUPPORTED, "size " + std::to_string(n) + " must be 13-smooth in 2..2^24");
+    const int64_t io = in_offsets ? in_offsets[i] : acc_in;
+    const int64_t oo = out_offsets ? out_offsets[i] : acc_out;
+    if (io < 0 || oo < 0) return fail(LFG_ERR_INVALID, "negative offset");
+    r.in_off.push_back(io);
+    r.out_off.push_back(oo);
+    r.in_span = std::max(r.in_span, io + n);
+    r.out_span = std::max(r.out_span, oo + n);
+    acc_in += n;
+    acc_out += n;
+  }
+  lfg::RaggedOptions opt;
+  opt.tile_target = tile_target();
+  if (tuning) {
+    if (tuning->tile_target >= 16) opt.tile_target = tuning->tile_target;
+    if (tuning->single_max >= 2) opt.single_max = tuning->single_max;
+    for (int j = 0; j < tuning->n_over; ++j) {
+      const int np = tuning->over_npass[j];
+      if (np < 1 || np > lfg::kMaxPass) return fail(LFG_ERR_INVALID, "bad override pass count");
+      opt.radices[tuning->over_n[j]] =
+          std::vector<int>(tuning->over_radices + 24 * j, tuning->over_radices + 24 * j + np);
+    }
+  }
+  opt.single_max = std::min<int64_t>(opt.single_max, lfg::max_single_group(precision));
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  r.device = dev;
+  if (!r.empty) {
+    e = lfg::prepare_group_kernels_f64();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel set-up");
+    r.options = opt;
+    std::string msg = lfg::build_ragged(r, opt);
+    if (!msg.empty()) {
+      lfg::free_ragged(r);
+      return fail(LFG_ERR_UNSUPPORTED, msg);
+    }
+  }
+  lfg_ragged* h = new (std::nothrow) lfg_ragged;
+  if (!h) {
+    lfg::free_ragged(r);
+    return fail(LFG_ERR_NOMEM, "host allocation");
+  }
+  h->r = std::move(r);
+  *out = h;
+  return LFG_OK;
+}
+
+lfg_status lfg_execute_ragged(const lfg_ragged* plan, const void* in, void* out, void* stream) {
+  if (!plan) return fail(LFG_ERR_INVALID, "null plan");
+  if (plan->r.empty) return LFG_OK;
+  if (!in || !out) return fail(LFG_ERR_INVALID, "null buffer");
+  if (in == out) return fail(LFG_ERR_UNSUPPORTED, "ragged batches run out of place");
+  cudaError_t e = lfg::execute_ragged(plan->r, in, out, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "execute ragged");
+  return LFG_OK;
+}
+
+lfg_status lfg_execute_ragged_host(const lfg_ragged* plan, const void* in, void* out) {
+  if (!plan) return fail(LFG_ERR_INVALID, "null plan");
+  const lfg::RaggedPlan& r = plan->r;
+  if (r.empty) return LFG_OK;
+  if (!in || !out || in == out) return fail(LFG_ERR_INVALID, "bad buffers");
+  const size_t es = r.precision == 0 ? 16 : 8;
+  const size_t ib = (size_t)r.in_span * es, ob = (size_t)r.out_span * es;
+  cudaError_t e;
+  if (!r.d_host_in) {
+    if ((e = cudaMalloc(&r.d_host_in, ib)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    if ((e = cudaMalloc(&r.d_host_out, ob)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+  }
+  if ((e = cudaMemcpy(r.d_host_in, in, ib, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(e, "host-to-device copy");
+  if ((e = cudaMemcpy(r.d_host_out, out, ob, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_fail(e, "host-to-device copy");
+  if ((e = lfg::execute_ragged(r, r.d_host_in, r.d_host_out, 0)) != cudaSuccess)
+    return cuda_fail(e, "execute ragged");
+  if ((e = cudaMemcpy(out, r.d_host_out, ob, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_fail(e, "device-to-host copy");
+  return LFG_OK;
+}
+
+void lfg_destroy_ragged(lfg_ragged* plan) {
+  if (!plan) return;
+  lfg::free_ragged(plan->r);
+  delete plan;
+}
+
+lfg_status lfg_get_ragged_info(const lfg_ragged* plan, lfg_ragged_info* info) {
+  if (!plan || !info) return fail(LFG_ERR_INVALID, "null argument");
+  const lfg::RaggedPlan& r = plan->r;
+  std::memset(info, 0, sizeof *info);
+  info->count = (int64_t)r.sizes.size();
+  info->classes = (int64_t)r.class_n.size();
+  info->items = (int64_t)r.items_host.size();
+  info->grid = r.launch.grid;
+  info->smem_bytes = (int64_t)r.launch.smem;
+  int64_t launches = 1;
+  if (r.per_size_mode) {
+    launches = 0;
+    for (const auto& L : r.per_size) launches += L.ngroups;
+  }
+  info->launches = r.empty ? 0 : launches;
+  const int64_t es = r.precision == 0 ? 16 : 8;
+  info->in_bytes = r.in_span * es;
+  info->out_bytes = r.out_span * es;
+  for (int64_t n : r.sizes) info->points += n;
+  info->flops = r.flops;
+  return LFG_OK;
+}
+
+lfg_status lfg_get_ragged_radices(const lfg_ragged* plan, int64_t n, int* radices, int* npass) {
+  if (!plan || !radices || !npass) return fail(LFG_ERR_INVALID, "null argument");
+  const lfg::RaggedPlan& r = plan->r;
+  *npass = 0;
+  for (size_t c = 0; c < r.class_n.size(); ++c)
+    if (r.class_n[c] == n) {
+      *npass = (int)r.class_radices[c].size();
+      for (int i = 0; i < *npass; ++i) radices[i] = r.class_radices[c][i];
+    }
   return LFG_OK;
 }
 

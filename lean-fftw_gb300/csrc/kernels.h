@@ -10,11 +10,18 @@ namespace lfg {
 
 constexpr int kGroupThreads = 256;             // threads per CTA of the group kernels
 constexpr size_t kMaxSmemBytes = 232448;       // opt-in shared memory per CTA on sm_103
+constexpr size_t kSmemBudget = kMaxSmemBytes - 1024;  // dynamic part planned (static smem aside)
 
 // FP64 group kernel: 2 * C * M * 16 bytes of shared memory.
 size_t group_smem_bytes_f64(const GroupDesc& g);
 cudaError_t prepare_group_kernels_f64();
 cudaError_t launch_group_f64(const GroupDesc& g, bool fwd, const void* in, void* out,
                              cudaStream_t stream);
+
+// Persistent FP64 kernel over a ragged batch (one launch for all sizes).
+size_t ragged_smem_bytes_f64(const RaggedClass& c);
+int ragged_blocks_per_sm_f64(size_t smem);
+cudaError_t launch_ragged_f64(const RaggedLaunch& r, bool fwd, const void* in, void* out,
+                              cudaStream_t stream);
 
 }  // namespace lfg

@@ -55,6 +55,28 @@ double plan_ops(int64_t n, const std::vector<int>& radices);
 // radices are set.  Returns an error message, or "" on success.
 std::string build_c2c(Plan& p, int64_t tile_target);
 
+// Pass twiddle tables of a radix sequence (host copy; pass 0 has none), with each pass's ns.
+struct PassTables {
+  std::vector<double> values;
+  std::vector<size_t> offset;
+  std::vector<int64_t> ns;
+};
+PassTables make_pass_tables(int64_t N, bool fwd, const std::vector<int>& rs, int precision);
+
+bool radix_ok(int R);
+std::string check_radices(int64_t N, const std::vector<int>& rs);
+int64_t divisor_at_most(int64_t n, int64_t cap);
+size_t smem_bytes(int64_t C, int64_t M, int precision);
+int64_t max_single_group(int precision);
+// Index after the last pass of the first group (rs.size() for a single group), balancing the
+// two groups' lengths, both at most max_m; -1 if impossible.
+int split_point(int64_t N, const std::vector<int>& rs, int64_t max_m);
+// Fill the passes and tile size of a group covering passes t0..t1-1; tw_base is the device
+// copy of PassTables::values.
+void fill_group(GroupDesc& g, const std::vector<int>& rs, const PassTables& pt, int t0, int t1,
+                int64_t nsub, int64_t tile_target, int precision, const void* tw_base);
+void* upload_tables(const std::vector<double>& v, int precision, std::string* err);
+
 void free_plan_memory(Plan& p);
 
 cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream);

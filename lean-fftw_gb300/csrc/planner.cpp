@@ -19,7 +19,11 @@
 namespace lfg {
 namespace {
 
+}  // namespace
+
 bool radix_ok(int R) { return R >= 2 && R <= kMaxRadix && kOpsUntw[R] > 0; }
+
+namespace {
 
 // per-point operations of a twiddled pass of radix R
 double tw_cost(int R) { return (double)kOpsTw[R] / R; }
@@ -54,6 +58,8 @@ const Best& best_tail(int64_t m, std::map<int64_t, Best>& memo) {
   return memo[m] = b;
 }
 
+}  // namespace
+
 // Largest divisor of n that is <= cap (at least 1).
 int64_t divisor_at_most(int64_t n, int64_t cap) {
   if (cap >= n) return n;
@@ -65,8 +71,6 @@ int64_t divisor_at_most(int64_t n, int64_t cap) {
 size_t smem_bytes(int64_t C, int64_t M, int precision) {
   return 2 * (size_t)C * (size_t)M * (precision == 0 ? 16 : 8);
 }
-
-}  // namespace
 
 std::vector<int> choose_radices(int64_t n, int precision) {
   (void)precision;
@@ -107,12 +111,69 @@ void free_plan_memory(Plan& p) {
   if (cur != p.device) cudaSetDevice(cur);
 }
 
-std::string build_c2c(Plan& p, int64_t tile_target) {
-  const int64_t N = p.n;
-  const int prec = p.precision;
-  const size_t elem = prec == 0 ? 16 : 8;
-  const int64_t max_single = (int64_t)(kMaxSmemBytes / (2 * elem));
-  std::vector<int>& rs = p.radices;
+PassTables make_pass_tables(int64_t N, bool fwd, const std::vector<int>& rs, int precision) {
+  PassTables pt;
+  std::vector<double> tab = cos_sin_2pi_table((uint64_t)N);
+  pt.offset.assign(rs.size(), 0);
+  pt.ns.assign(rs.size(), 0);
+  size_t total = 0;
+  int64_t acc = 1;
+  for (size_t t = 0; t < rs.size(); ++t) {
+    pt.ns[t] = acc;
+    acc *= rs[t];
+    if (t == 0) continue;
+    pt.offset[t] = total;
+    total += 2 * (size_t)(rs[t] - 1) * pt.ns[t];
+    total = (total + 3) & ~(size_t)3;   // 32-byte aligned tables
+  }
+  pt.values.assign(total, 0.0);
+  for (size_t t = 1; t < rs.size(); ++t)
+    pass_twiddles(tab, fwd, (uint64_t)N, rs[t], (uint64_t)pt.ns[t], pt.values.data() + pt.offset[t]);
+  (void)precision;
+  return pt;
+}
+
+int split_point(int64_t N, const std::vector<int>& rs, int64_t max_m) {
+  if (N <= max_m) return (int)rs.size();
+  int best = -1;
+  int64_t bestv = INT64_MAX;
+  int64_t P = 1;
+  for (int t = 0; t + 1 < (int)rs.size(); ++t) {
+    P *= rs[t];
+    int64_t Q = N / P;
+    if (P > max_m || Q > max_m) continue;
+    int64_t v = std::max(P, Q);
+    if (v < bestv) { bestv = v; best = t + 1; }
+  }
+  return best;
+}
+
+void fill_group(GroupDesc& g, const std::vector<int>& rs, const PassTables& pt, int t0, int t1,
+                int64_t nsub, int64_t tile_target, int precision, const void* tw_base) {
+  int64_t M = 1;
+  for (int t = t0; t < t1; ++t) M *= rs[t];
+  g.M = (int)M;
+  g.npass = t1 - t0;
+  g.nsub = (int)nsub;
+  int64_t cmax = std::max<int64_t>(1, tile_target / M);
+  while (cmax > 1 && smem_bytes(cmax, M, precision) > kSmemBudget) --cmax;
+  g.C = (int)divisor_at_most(nsub, cmax);
+  int64_t P0 = 1;
+  for (int t = 0; t < t0; ++t) P0 *= rs[t];
+  g.kmul = (int)P0;
+  g.twsub = t0 > 0 ? 1 : 0;
+  for (int t = t0; t < t1; ++t) {
+    PassDesc& d = g.pass[t - t0];
+    d.R = rs[t];
+    d.ns_g = (int)pt.ns[t];
+    d.ns_loc = (int)(pt.ns[t] / P0);
+    if (t == 0) d.tw = nullptr;
+    else if (precision == 0) d.tw = (const double*)tw_base + pt.offset[t];
+    else d.tw = (const float*)tw_base + pt.offset[t];
+  }
+}
+
+std::string check_radices(int64_t N, const std::vector<int>& rs) {
   if (rs.empty()) return "no radix sequence";
   if ((int)rs.size() > kMaxPass) return "too many passes";
   int64_t prod = 1;
@@ -121,90 +182,65 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
     prod *= R;
   }
   if (prod != N) return "radices do not multiply to n";
+  return "";
+}
 
+void* upload_tables(const std::vector<double>& v, int precision, std::string* err) {
+  void* d = nullptr;
+  size_t bytes;
+  std::vector<float> v32;
+  const void* src;
+  if (precision == 0) {
+    bytes = std::max<size_t>(v.size(), 4) * sizeof(double);
+    src = v.data();
+  } else {
+    v32.assign(v.begin(), v.end());
+    v32.resize(std::max<size_t>(v32.size(), 4));
+    bytes = v32.size() * sizeof(float);
+    src = v32.data();
+  }
+  if (cudaMalloc(&d, bytes) != cudaSuccess) {
+    *err = "cudaMalloc of twiddle tables failed";
+    return nullptr;
+  }
+  if (!v.empty()) {
+    cudaError_t e = cudaMemcpy(d, src, std::min(bytes, (precision == 0 ? 8 : 4) * v.size()),
+                               cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      *err = std::string("twiddle upload: ") + cudaGetErrorString(e);
+      cudaFree(d);
+      return nullptr;
+    }
+  }
+  return d;
+}
+
+int64_t max_single_group(int precision) {
+  return (int64_t)(kSmemBudget / (2 * (precision == 0 ? 16 : 8)));
+}
+
+std::string build_c2c(Plan& p, int64_t tile_target) {
+  const int64_t N = p.n;
+  const int prec = p.precision;
+  std::vector<int>& rs = p.radices;
+  std::string msg = check_radices(N, rs);
+  if (!msg.empty()) return msg;
   // pass grouping: one group when a transform fits one CTA's shared memory, else split the
   // sequence after the prefix whose product P best balances P against N/P
-  int split = (int)rs.size();
-  if (N > max_single) {
-    int best = -1;
-    int64_t bestv = INT64_MAX;
-    int64_t P = 1;
-    for (int t = 0; t + 1 < (int)rs.size(); ++t) {
-      P *= rs[t];
-      int64_t Q = N / P;
-      if (P > max_single || Q > max_single) continue;
-      int64_t v = std::max(P, Q);
-      if (v < bestv) { bestv = v; best = t + 1; }
-    }
-    if (best < 0) return "size too large for two pass groups with this radix order";
-    split = best;
-  }
-
-  // twiddle tables of every pass t >= 1, concatenated (each 16-byte aligned)
-  std::vector<double> tab = cos_sin_2pi_table((uint64_t)N);
-  std::vector<size_t> toff(rs.size(), 0);
-  size_t total = 0;
-  std::vector<int64_t> ns(rs.size());
-  int64_t acc = 1;
-  for (size_t t = 0; t < rs.size(); ++t) {
-    ns[t] = acc;
-    acc *= rs[t];
-    if (t == 0) continue;
-    toff[t] = total;
-    total += 2 * (size_t)(rs[t] - 1) * ns[t];
-    total = (total + 1) & ~(size_t)1;
-  }
-  std::vector<double> host(std::max<size_t>(total, 2));
-  for (size_t t = 1; t < rs.size(); ++t)
-    pass_twiddles(tab, p.fwd, (uint64_t)N, rs[t], (uint64_t)ns[t], host.data() + toff[t]);
-  size_t tw_bytes;
-  std::vector<float> host32;
-  if (prec == 0) {
-    tw_bytes = host.size() * sizeof(double);
-  } else {
-    host32.assign(host.begin(), host.end());
-    tw_bytes = host32.size() * sizeof(float);
-  }
-  if (cudaMalloc(&p.d_twiddles, tw_bytes) != cudaSuccess) return "cudaMalloc of twiddle tables failed";
-  cudaError_t e = cudaMemcpy(p.d_twiddles, prec == 0 ? (const void*)host.data() : (const void*)host32.data(),
-                             tw_bytes, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return std::string("twiddle upload: ") + cudaGetErrorString(e);
-  auto tw_ptr = [&](size_t t) -> const void* {
-    if (t == 0) return nullptr;
-    return prec == 0 ? (const void*)((const double*)p.d_twiddles + toff[t])
-                     : (const void*)((const float*)p.d_twiddles + toff[t]);
-  };
-
-  auto make_group = [&](GroupDesc& g, int t0, int t1, int64_t nsub, int64_t nsub_div_hint) {
-    int64_t M = 1;
-    for (int t = t0; t < t1; ++t) M *= rs[t];
-    g.M = (int)M;
-    g.npass = t1 - t0;
-    g.nsub = (int)nsub;
-    int64_t cmax = std::max<int64_t>(1, tile_target / M);
-    while (cmax > 1 && smem_bytes(cmax, M, prec) > kMaxSmemBytes) --cmax;
-    g.C = (int)divisor_at_most(nsub_div_hint, cmax);
-    int64_t P0 = 1;
-    for (int t = 0; t < t0; ++t) P0 *= rs[t];
-    g.kmul = (int)P0;
-    g.twsub = t0 > 0 ? 1 : 0;
-    for (int t = t0; t < t1; ++t) {
-      PassDesc& d = g.pass[t - t0];
-      d.R = rs[t];
-      d.ns_g = (int)ns[t];
-      d.ns_loc = (int)(ns[t] / P0);
-      d.tw = tw_ptr(t);
-    }
-  };
+  const int split = split_point(N, rs, max_single_group(prec));
+  if (split < 0) return "size too large for two pass groups with this radix order";
+  PassTables pt = make_pass_tables(N, p.fwd, rs, prec);
+  p.d_twiddles = upload_tables(pt.values, prec, &msg);
+  if (!p.d_twiddles) return msg;
 
   p.flops = plan_ops(N, rs) * (double)p.howmany;
   if (split == (int)rs.size()) {
     p.ngroups = 1;
     GroupDesc& g = p.groups[0];
+    fill_group(g, rs, pt, 0, (int)rs.size(), 1, tile_target, prec, p.d_twiddles);
     // lines may share a tile; pick C by the target only (the batch need not divide)
-    make_group(g, 0, (int)rs.size(), 1, 1);
     int64_t cmax = std::max<int64_t>(1, tile_target / N);
-    while (cmax > 1 && smem_bytes(cmax, N, prec) > kMaxSmemBytes) --cmax;
+    while (cmax > 1 && smem_bytes(cmax, N, prec) > kSmemBudget) --cmax;
     g.C = (int)std::min<int64_t>(cmax, std::max<int64_t>(1, p.howmany));
     g.total_sub = p.howmany;
     g.in_line = p.in.dist;
@@ -221,8 +257,8 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
     const int64_t Q = N / P;
     GroupDesc& g1 = p.groups[0];
     GroupDesc& g2 = p.groups[1];
-    make_group(g1, 0, split, Q, Q);
-    make_group(g2, split, (int)rs.size(), P, P);
+    fill_group(g1, rs, pt, 0, split, Q, tile_target, prec, p.d_twiddles);
+    fill_group(g2, rs, pt, split, (int)rs.size(), P, tile_target, prec, p.d_twiddles);
     g1.total_sub = p.howmany * Q;
     g2.total_sub = p.howmany * P;
     // group 1: sub-problem b reads x[b + Q*i], writes z[b*P + m]; the intermediate z

@@ -1,0 +1,294 @@
+// Ragged batches: many 1-D complex transforms of different 13-smooth sizes in one launch.
+//
+// lean-fftw plans and runs one transform at a time (bench/backends/bench-leanfftw.c:270-291);
+// its planner measures every candidate schedule per size on the CPU
+// (LeanFFTW/Asm/Planner.lean:209-286).  Here a ragged batch is planned once: transforms are
+// grouped by size ("classes"), each class gets a radix sequence and a tile shape, and the
+// work is cut into items (a tile of same-size transforms, or one whole two-group transform)
+// that a persistent kernel pulls from a queue, largest first.  The queue reset and the
+// kernel are captured in a CUDA graph and replayed.
+//
+// Every transform performs the reference passes of its radix sequence, so each output is
+// bit-identical to lean-fftw's refTransform for that size and sequence.
+#include "ragged.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <numeric>
+
+#include "generated/opcounts.h"
+#include "kernels.h"
+
+namespace lfg {
+
+void free_ragged(RaggedPlan& r) {
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != r.device) cudaSetDevice(r.device);
+  if (r.graph_exec) cudaGraphExecDestroy(r.graph_exec);
+  if (r.capture_stream) cudaStreamDestroy(r.capture_stream);
+  for (void* p : {r.d_twiddles, r.d_classes, r.d_items, r.d_in_off, r.d_out_off, r.d_counter,
+                  r.d_host_in, r.d_host_out})
+    if (p) cudaFree(p);
+  r.graph_exec = nullptr;
+  r.capture_stream = nullptr;
+  r.d_twiddles = r.d_classes = r.d_items = r.d_in_off = r.d_out_off = r.d_counter = nullptr;
+  r.d_host_in = r.d_host_out = nullptr;
+  if (cur != r.device) cudaSetDevice(cur);
+}
+
+std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
+  const int prec = r.precision;
+  const int64_t count = (int64_t)r.sizes.size();
+  // classes in increasing size; lines sorted by (size, original index)
+  std::vector<int64_t> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t a, int64_t b) { return r.sizes[a] < r.sizes[b]; });
+  r.line_order = order;
+  std::vector<int64_t> in_sorted(count), out_sorted(count);
+  for (int64_t i = 0; i < count; ++i) {
+    in_sorted[i] = r.in_off[order[i]];
+    out_sorted[i] = r.out_off[order[i]];
+  }
+  // distinct sizes
+  r.class_n.clear();
+  r.class_first.clear();
+  r.class_count.clear();
+  for (int64_t i = 0; i < count; ++i) {
+    int64_t n = r.sizes[order[i]];
+    if (r.class_n.empty() || r.class_n.back() != n) {
+      r.class_n.push_back(n);
+      r.class_first.push_back(i);
+      r.class_count.push_back(0);
+    }
+    r.class_count.back()++;
+  }
+  const int ncls = (int)r.class_n.size();
+  r.class_radices.assign(ncls, {});
+  r.classes_host.assign(ncls, RaggedClass{});
+
+  // radix sequences and twiddle tables of every class, in one device buffer
+  std::vector<PassTables> tables(ncls);
+  std::vector<size_t> base(ncls, 0);
+  size_t total = 0;
+  r.flops = 0;
+  for (int c = 0; c < ncls; ++c) {
+    const int64_t n = r.class_n[c];
+    auto it = opt.radices.find(n);
+    r.class_radices[c] = it != opt.radices.end() ? it->second : choose_radices(n, prec);
+    std::string msg = check_radices(n, r.class_radices[c]);
+    if (!msg.empty()) return "size " + std::to_string(n) + ": " + msg;
+    tables[c] = make_pass_tables(n, r.fwd, r.class_radices[c], prec);
+    base[c] = total;
+    total += tables[c].values.size();
+    r.flops += plan_ops(n, r.class_radices[c]) * (double)r.class_count[c];
+  }
+  std::vector<double> all(total);
+  for (int c = 0; c < ncls; ++c)
+    std::copy(tables[c].values.begin(), tables[c].values.end(), all.begin() + base[c]);
+  std::string err;
+  r.d_twiddles = upload_tables(all, prec, &err);
+  if (!r.d_twiddles) return err;
+  const size_t scal = prec == 0 ? sizeof(double) : sizeof(float);
+
+  // groups and work items
+  std::vector<RaggedItem> items;
+  std::vector<double> item_cost;
+  size_t smem = 0;
+  for (int c = 0; c < ncls; ++c) {
+    const int64_t n = r.class_n[c];
+    const std::vector<int>& rs = r.class_radices[c];
+    RaggedClass& rc = r.classes_host[c];
+    rc.n = (int)n;
+    const void* tw = static_cast<const char*>(r.d_twiddles) + base[c] * scal;
+    int split = split_point(n, rs, opt.single_max);
+    if (split < 0) return "size " + std::to_string(n) + " needs more than two pass groups";
+    const double ops_one = plan_ops(n, rs);
+    if (split == (int)rs.size()) {
+      rc.ngroups = 1;
+      GroupDesc& g = rc.g[0];
+      fill_group(g, rs, tables[c], 0, (int)rs.size(), 1, opt.tile_target, prec, tw);
+      int64_t cmax = std::max<int64_t>(1, opt.tile_target / n);
+      while (cmax > 1 && smem_bytes(cmax, n, prec) > kSmemBudget) --cmax;
+      g.C = (int)std::min<int64_t>(cmax, r.class_count[c]);
+      g.in_sub = g.out_sub = 0;
+      g.in_elem = g.out_elem = 1;
+      g.total_sub = g.C;
+      for (int64_t i = 0; i < r.class_count[c]; i += g.C) {
+        int cnt = (int)std::min<int64_t>(g.C, r.class_count[c] - i);
+        items.push_back(RaggedItem{c, cnt, r.class_first[c] + i});
+        item_cost.push_back(ops_one * cnt);
+      }
+    } else {
+      rc.ngroups = 2;
+      int64_t P = 1;
+      for (int t = 0; t < split; ++t) P *= rs[t];
+      const int64_t Q = n / P;
+      GroupDesc& g1 = rc.g[0];
+      GroupDesc& g2 = rc.g[1];
+      fill_group(g1, rs, tables[c], 0, split, Q, opt.tile_target, prec, tw);
+      fill_group(g2, rs, tables[c], split, (int)rs.size(), P, opt.tile_target, prec, tw);
+      // group 1: x[b + Q i] -> out[b P + m]; group 2: out[i P + m] -> out[o P + m]
+      g1.in_sub = 1;
+      g1.in_elem = Q;
+      g1.out_sub = P;
+      g1.out_elem = 1;
+      g2.in_sub = 1;
+      g2.in_elem = P;
+      g2.out_sub = 1;
+      g2.out_elem = P;
+      g1.total_sub = Q;
+      g2.total_sub = P;
+      for (int64_t i = 0; i < r.class_count[c]; ++i) {
+        items.push_back(RaggedItem{c, 1, r.class_first[c] + i});
+        item_cost.push_back(ops_one);
+      }
+    }
+    for (int gi = 0; gi < rc.ngroups; ++gi) smem = std::max(smem, smem_bytes(rc.g[gi].C, rc.g[gi].M, prec));
+  }
+  // largest items first
+  std::vector<size_t> perm(items.size());
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [&](size_t a, size_t b) { return item_cost[a] > item_cost[b]; });
+  r.items_host.resize(items.size());
+  for (size_t i = 0; i < perm.size(); ++i) r.items_host[i] = items[perm[i]];
+
+  // device copies
+  auto up = [&](void** d, const void* h, size_t bytes) -> bool {
+    if (cudaMalloc(d, std::max<size_t>(bytes, 16)) != cudaSuccess) return false;
+    return bytes == 0 || cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  if (!up(&r.d_classes, r.classes_host.data(), r.classes_host.size() * sizeof(RaggedClass)) ||
+      !up(&r.d_items, r.items_host.data(), r.items_host.size() * sizeof(RaggedItem)) ||
+      !up(&r.d_in_off, in_sorted.data(), in_sorted.size() * sizeof(int64_t)) ||
+      !up(&r.d_out_off, out_sorted.data(), out_sorted.size() * sizeof(int64_t)) ||
+      cudaMalloc(&r.d_counter, 256) != cudaSuccess)
+    return "device allocation for the ragged plan failed";
+  cudaMemset(r.d_counter, 0, 256);
+
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, r.device);
+  r.launch.classes = static_cast<const RaggedClass*>(r.d_classes);
+  r.launch.items = static_cast<const RaggedItem*>(r.d_items);
+  r.launch.nitems = (int)r.items_host.size();
+  r.launch.in_off = static_cast<const int64_t*>(r.d_in_off);
+  r.launch.out_off = static_cast<const int64_t*>(r.d_out_off);
+  r.launch.counter = static_cast<unsigned*>(r.d_counter);
+  r.launch.smem = smem;
+  const int per_sm = prec == 0 ? ragged_blocks_per_sm_f64(smem) : 1;
+  const int64_t want = (int64_t)prop.multiProcessorCount * per_sm;
+  r.launch.grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)r.items_host.size()));
+
+  // per-size strategy (the comparison point): one batched launch per distinct size when the
+  // class's lines are evenly spaced in both buffers, else one launch per transform
+  r.per_size.clear();
+  for (int c = 0; c < ncls; ++c) {
+    const int64_t n = r.class_n[c];
+    const int64_t f = r.class_first[c], k = r.class_count[c];
+    bool even = true;
+    int64_t din = k > 1 ? in_sorted[f + 1] - in_sorted[f] : n;
+    int64_t dout = k > 1 ? out_sorted[f + 1] - out_sorted[f] : n;
+    for (int64_t i = 1; i < k && even; ++i)
+      even = in_sorted[f + i] - in_sorted[f + i - 1] == din && out_sorted[f + i] - out_sorted[f + i - 1] == dout;
+    even = even && din > 0 && dout > 0;
+    const std::vector<int>& rs = r.class_radices[c];
+    const void* tw = static_cast<const char*>(r.d_twiddles) + base[c] * scal;
+    const int64_t lines = even ? k : 1;
+    for (int64_t i = 0; i < (even ? 1 : k); ++i) {
+      PerSizeLaunch L;
+      L.in_base = in_sorted[f + i];
+      L.out_base = out_sorted[f + i];
+      int split = split_point(n, rs, max_single_group(prec));
+      if (split == (int)rs.size()) {
+        L.ngroups = 1;
+        GroupDesc& g = L.g[0];
+        fill_group(g, rs, tables[c], 0, (int)rs.size(), 1, opt.tile_target, prec, tw);
+        int64_t cmax = std::max<int64_t>(1, opt.tile_target / n);
+        while (cmax > 1 && smem_bytes(cmax, n, prec) > kSmemBudget) --cmax;
+        g.C = (int)std::min<int64_t>(cmax, lines);
+        g.total_sub = lines;
+        g.in_line = din;
+        g.out_line = dout;
+        g.in_sub = g.out_sub = 0;
+        g.in_elem = g.out_elem = 1;
+      } else {
+        L.ngroups = 2;
+        int64_t P = 1;
+        for (int t = 0; t < split; ++t) P *= rs[t];
+        const int64_t Q = n / P;
+        fill_group(L.g[0], rs, tables[c], 0, split, Q, opt.tile_target, prec, tw);
+        fill_group(L.g[1], rs, tables[c], split, (int)rs.size(), P, opt.tile_target, prec, tw);
+        L.g[0].total_sub = lines * Q;
+        L.g[1].total_sub = lines * P;
+        L.g[0].in_line = din;
+        L.g[0].in_sub = 1;
+        L.g[0].in_elem = Q;
+        L.g[0].out_line = dout;
+        L.g[0].out_sub = P;
+        L.g[0].out_elem = 1;
+        L.g[1].in_line = dout;
+        L.g[1].in_sub = 1;
+        L.g[1].in_elem = P;
+        L.g[1].out_line = dout;
+        L.g[1].out_sub = 1;
+        L.g[1].out_elem = P;
+      }
+      r.per_size.push_back(L);
+    }
+  }
+  return "";
+}
+
+cudaError_t execute_ragged_direct(const RaggedPlan& r, const void* in, void* out, cudaStream_t s) {
+  if (r.per_size_mode) {
+    const size_t es = r.precision == 0 ? 16 : 8;
+    for (const PerSizeLaunch& L : r.per_size) {
+      const char* ib = static_cast<const char*>(in) + L.in_base * es;
+      char* ob = static_cast<char*>(out) + L.out_base * es;
+      for (int gi = 0; gi < L.ngroups; ++gi) {
+        cudaError_t e = launch_group_f64(L.g[gi], r.fwd, gi == 0 ? (const void*)ib : (const void*)ob, ob, s);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    return cudaSuccess;
+  }
+  cudaError_t e = cudaMemsetAsync(r.d_counter, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  return launch_ragged_f64(r.launch, r.fwd, in, out, s);
+}
+
+cudaError_t execute_ragged(const RaggedPlan& r, const void* in, void* out, cudaStream_t s) {
+  if (r.empty) return cudaSuccess;
+  if (!r.use_graph) return execute_ragged_direct(r, in, out, s);
+  if (!r.graph_exec || r.graph_in != in || r.graph_out != out) {
+    // capture the queue reset and the launch(es) on a private stream, then replay
+    if (r.graph_exec) {
+      cudaGraphExecDestroy(r.graph_exec);
+      r.graph_exec = nullptr;
+    }
+    if (!r.capture_stream) {
+      cudaError_t e = cudaStreamCreateWithFlags(&r.capture_stream, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return e;
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(r.capture_stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t e2 = execute_ragged_direct(r, in, out, r.capture_stream);
+    e = cudaStreamEndCapture(r.capture_stream, &graph);
+    if (e2 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return e2;
+    }
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(&r.graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return e;
+    r.graph_in = in;
+    r.graph_out = out;
+  }
+  return cudaGraphLaunch(r.graph_exec, s);
+}
+
+}  // namespace lfg

@@ -1,0 +1,59 @@
+// Host-side ragged-batch plan (see ragged.cpp).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "plan.h"
+#include "stockham.h"
+
+namespace lfg {
+
+struct RaggedOptions {
+  int64_t tile_target = 2048;      // complex elements per CTA tile
+  int64_t single_max = 2048;       // largest size run as one pass group
+  std::map<int64_t, std::vector<int>> radices;   // per-size overrides (autotuner)
+};
+
+// One launch of the per-size strategy: a batched plan over one size's evenly spaced lines.
+struct PerSizeLaunch {
+  GroupDesc g[2];
+  int ngroups = 1;
+  int64_t in_base = 0, out_base = 0;   // complex-element offsets of the first line
+};
+
+struct RaggedPlan {
+  int precision = 0;
+  bool fwd = true;
+  int device = 0;
+  bool empty = false;
+  bool use_graph = true;
+  bool per_size_mode = false;
+  std::vector<int64_t> sizes, in_off, out_off;        // as given (complex elements)
+  std::vector<int64_t> line_order;                     // lines sorted by size
+  std::vector<int64_t> class_n, class_first, class_count;
+  std::vector<std::vector<int>> class_radices;
+  std::vector<RaggedClass> classes_host;
+  std::vector<RaggedItem> items_host;
+  std::vector<PerSizeLaunch> per_size;
+  RaggedLaunch launch{};
+  int64_t in_span = 0, out_span = 0;                   // complex elements
+  double flops = 0;
+  RaggedOptions options;
+  void *d_twiddles = nullptr, *d_classes = nullptr, *d_items = nullptr, *d_in_off = nullptr,
+       *d_out_off = nullptr, *d_counter = nullptr;
+  mutable void *d_host_in = nullptr, *d_host_out = nullptr;
+  mutable cudaGraphExec_t graph_exec = nullptr;
+  mutable cudaStream_t capture_stream = nullptr;
+  mutable const void* graph_in = nullptr;
+  mutable void* graph_out = nullptr;
+};
+
+std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt);
+cudaError_t execute_ragged(const RaggedPlan& r, const void* in, void* out, cudaStream_t s);
+void free_ragged(RaggedPlan& r);
+
+}  // namespace lfg

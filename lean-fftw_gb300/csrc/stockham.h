@@ -54,4 +54,32 @@ struct GroupDesc {
   PassDesc pass[kMaxPass];
 };
 
+// One distinct size of a ragged batch: one group, or two groups run back to back by one CTA
+// (first group to the output, second group in place on the output).  Line strides of the
+// GroupDescs are unused; lines are located through per-transform offsets.
+struct RaggedClass {
+  GroupDesc g[2];
+  int ngroups;
+  int n;
+};
+
+// A work item: `count` transforms of class `cls`, the lines first .. first+count-1 of the
+// offset lists (sorted by class).
+struct RaggedItem {
+  int cls;
+  int count;
+  int64_t first;
+};
+
+struct RaggedLaunch {
+  const RaggedClass* classes;
+  const RaggedItem* items;
+  int nitems;
+  const int64_t* in_off;
+  const int64_t* out_off;
+  unsigned int* counter;
+  unsigned grid;
+  size_t smem;
+};
+
 }  // namespace lfg

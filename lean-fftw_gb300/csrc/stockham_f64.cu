@@ -13,110 +13,13 @@
 // the FP64 pipe fed, which a few warps per SM do.
 #include <cuda_runtime.h>
 
-#include "generated/codelets_f64.cuh"
-#include "kernels.h"
-#include "stockham.h"
+#include <algorithm>
+
+#include "stockham_f64.cuh"
 
 namespace lfg {
+using namespace dev;
 namespace {
-
-// One pass over the C sub-problems of a tile: src, dst are tile buffers in shared memory.
-template <bool FWD, int R, bool TW>
-__device__ __forceinline__ void pass_f64(const double2* __restrict__ src, double2* __restrict__ dst,
-                                         int C, int M, const PassDesc& pd, int kmul, int64_t msub0) {
-  const int MR = M / R;
-  const int nb = C * MR;
-  const int ns = pd.ns_loc;
-  const double* __restrict__ tw = static_cast<const double*>(pd.tw);
-  const int64_t nsg = pd.ns_g;
-  for (int q = threadIdx.x; q < nb; q += blockDim.x) {
-    const int c = q / MR;
-    const int j = q - c * MR;
-    double x[TW ? 4 * R - 2 : 2 * R];
-    double y[2 * R];
-    const double2* s = src + c * M + j;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const double2 v = s[r * MR];
-      x[2 * r] = v.x;
-      x[2 * r + 1] = v.y;
-    }
-    const int k = j % ns;
-    if (TW) {
-      // table index of the twiddle: k_loc * kmul + sub-problem index (second group only)
-      const int64_t kg = (int64_t)k * kmul + (msub0 >= 0 ? msub0 + c : 0);
-#pragma unroll
-      for (int r = 0; r < R - 1; ++r) {
-        x[2 * R + 2 * r] = __ldg(tw + 2 * r * nsg + kg);
-        x[2 * R + 2 * r + 1] = __ldg(tw + (2 * r + 1) * nsg + kg);
-      }
-    }
-    BflyD<FWD, R, TW>::run(x, y);
-    const int b = j / ns;
-    double2* d = dst + c * M + b * ns * R + k;
-#pragma unroll
-    for (int r = 0; r < R; ++r) d[r * ns] = make_double2(y[2 * r], y[2 * r + 1]);
-  }
-}
-
-template <bool FWD>
-__device__ __forceinline__ void run_pass_f64(const double2* src, double2* dst, int C, int M,
-                                             const PassDesc& pd, int kmul, int64_t msub0) {
-#define LFG_PASS_CASE(RR)                                                   \
-  case RR:                                                                  \
-    if (pd.tw) pass_f64<FWD, RR, true>(src, dst, C, M, pd, kmul, msub0);    \
-    else pass_f64<FWD, RR, false>(src, dst, C, M, pd, kmul, msub0);         \
-    break;
-  switch (pd.R) {
-    LFG_PASS_CASE(2)
-    LFG_PASS_CASE(3)
-    LFG_PASS_CASE(4)
-    LFG_PASS_CASE(5)
-    LFG_PASS_CASE(6)
-    LFG_PASS_CASE(7)
-    LFG_PASS_CASE(8)
-    LFG_PASS_CASE(9)
-    LFG_PASS_CASE(10)
-    LFG_PASS_CASE(11)
-    LFG_PASS_CASE(12)
-    LFG_PASS_CASE(13)
-    LFG_PASS_CASE(14)
-    LFG_PASS_CASE(15)
-    LFG_PASS_CASE(16)
-    default: break;   // rejected by the planner
-  }
-#undef LFG_PASS_CASE
-}
-
-// Copy a tile between global memory and a shared-memory tile buffer; the loop order makes
-// consecutive threads touch consecutive global addresses (elements of a sub-problem when
-// they are contiguous, else neighbouring sub-problems).
-template <bool LOAD>
-__device__ __forceinline__ void copy_tile(double2* tile, const double2* gin, double2* gout,
-                                          const GroupDesc& g, int64_t s0, int C) {
-  const int64_t line_st = LOAD ? g.in_line : g.out_line;
-  const int64_t sub_st = LOAD ? g.in_sub : g.out_sub;
-  const int64_t elem_st = LOAD ? g.in_elem : g.out_elem;
-  const int M = g.M;
-  const int n = C * M;
-  const bool elem_fast = (elem_st == 1);
-  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
-    int c, i;
-    if (elem_fast) {
-      c = idx / M;
-      i = idx - c * M;
-    } else {
-      i = idx / C;
-      c = idx - i * C;
-    }
-    const int64_t s = s0 + c;
-    const int64_t line = s / g.nsub;
-    const int64_t sub = s - line * g.nsub;
-    const int64_t a = line * line_st + sub * sub_st + (int64_t)i * elem_st;
-    if (LOAD) tile[c * M + i] = gin[a];
-    else gout[a] = tile[c * M + i];
-  }
-}
 
 template <bool FWD>
 __global__ void __launch_bounds__(kGroupThreads)
@@ -125,35 +28,97 @@ group_kernel_f64(const GroupDesc g, const double2* in, double2* out) {
   const int64_t s0 = (int64_t)blockIdx.x * g.C;
   const int64_t rem = g.total_sub - s0;
   const int C = rem < g.C ? (int)rem : g.C;
-  double2* A = smem_f64;
-  double2* B = smem_f64 + (size_t)g.C * g.M;
-  copy_tile<true>(A, in, nullptr, g, s0, C);
-  __syncthreads();
-  // second group: the sub-problem index within the line enters the twiddle index
-  const int64_t msub0 = g.twsub ? (s0 % g.nsub) : -1;
-  for (int t = 0; t < g.npass; ++t) {
-    run_pass_f64<FWD>(A, B, C, g.M, g.pass[t], g.kmul, msub0);
+  process_tile_f64<FWD>(g, StridedLines{g.in_line, g.out_line}, s0, C, in, out, smem_f64);
+}
+
+// Persistent kernel over a ragged batch: each CTA takes work items from a queue (an atomic
+// ticket counter, zeroed before the launch) until it is empty.  An item is a tile of up to
+// C transforms of one size (one group), or one whole transform of a two-group size, whose
+// first group writes its intermediate to the output and whose second group then works on
+// the output in place; the barrier between them orders the global-memory traffic within
+// the CTA.  Items are sorted by decreasing cost, so the largest start first.
+template <bool FWD>
+__global__ void __launch_bounds__(kGroupThreads)
+ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __restrict__ items,
+                  int nitems, const int64_t* __restrict__ in_off,
+                  const int64_t* __restrict__ out_off, const double2* in, double2* out,
+                  unsigned int* counter) {
+  extern __shared__ double2 smem_f64[];
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
     __syncthreads();
-    double2* tmp = A;
-    A = B;
-    B = tmp;
+    const int it = s_item;
+    if (it >= nitems) break;
+    const RaggedItem w = items[it];
+    const RaggedClass& rc = classes[w.cls];
+    const ListedLines lines{in_off, out_off, w.first};
+    if (rc.ngroups == 1) {
+      process_tile_f64<FWD>(rc.g[0], lines, 0, w.count, in, out, smem_f64);
+    } else {
+      const GroupDesc& g1 = rc.g[0];
+      const GroupDesc& g2 = rc.g[1];
+      for (int64_t s0 = 0; s0 < g1.nsub; s0 += g1.C) {
+        process_tile_f64<FWD>(g1, lines, s0, g1.C, in, out, smem_f64);
+        __syncthreads();
+      }
+      // the second group reads the first group's result from the output
+      const ListedLines inner{out_off, out_off, w.first};
+      for (int64_t s0 = 0; s0 < g2.nsub; s0 += g2.C) {
+        process_tile_f64<FWD>(g2, inner, s0, g2.C, out, out, smem_f64);
+        __syncthreads();
+      }
+    }
+    __syncthreads();   // every thread has read s_item before it is overwritten
   }
-  copy_tile<false>(A, nullptr, out, g, s0, C);
 }
 
 }  // namespace
 
 size_t group_smem_bytes_f64(const GroupDesc& g) { return 2 * (size_t)g.C * g.M * sizeof(double2); }
 
-cudaError_t prepare_group_kernels_f64() {
-  // the opt-in shared-memory limit is a property of the function in the current device's
-  // context; the planner calls this once per plan, on the plan's device
-  cudaError_t e = cudaFuncSetAttribute(group_kernel_f64<true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kMaxSmemBytes);
+size_t ragged_smem_bytes_f64(const RaggedClass& c) {
+  size_t m = 0;
+  for (int i = 0; i < c.ngroups; ++i) m = std::max(m, group_smem_bytes_f64(c.g[i]));
+  return m;
+}
+
+cudaError_t launch_ragged_f64(const RaggedLaunch& r, bool fwd, const void* in, void* out,
+                              cudaStream_t stream) {
+  if (r.nitems <= 0) return cudaSuccess;
+  auto kern = fwd ? ragged_kernel_f64<true> : ragged_kernel_f64<false>;
+  kern<<<r.grid, kGroupThreads, r.smem, stream>>>(
+      r.classes, r.items, r.nitems, r.in_off, r.out_off, static_cast<const double2*>(in),
+      static_cast<double2*>(out), r.counter);
+  return cudaGetLastError();
+}
+
+int ragged_blocks_per_sm_f64(size_t smem) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ragged_kernel_f64<true>, kGroupThreads,
+                                                    smem) != cudaSuccess)
+    return 1;
+  return nb > 0 ? nb : 1;
+}
+
+// The opt-in shared-memory limit is a property of a function in the current device's
+// context: allow each kernel the per-CTA maximum minus its static shared memory.  The planner
+// calls this once per plan, on the plan's device.
+template <class K>
+cudaError_t allow_max_smem(K kern) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, kern);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(group_kernel_f64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kMaxSmemBytes);
+  return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(kMaxSmemBytes - a.sharedSizeBytes));
+}
+
+cudaError_t prepare_group_kernels_f64() {
+  cudaError_t e;
+  if ((e = allow_max_smem(group_kernel_f64<true>)) != cudaSuccess) return e;
+  if ((e = allow_max_smem(group_kernel_f64<false>)) != cudaSuccess) return e;
+  if ((e = allow_max_smem(ragged_kernel_f64<true>)) != cudaSuccess) return e;
+  return allow_max_smem(ragged_kernel_f64<false>);
 }
 
 cudaError_t launch_group_f64(const GroupDesc& g, bool fwd, const void* in, void* out,

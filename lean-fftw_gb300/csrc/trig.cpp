@@ -6,7 +6,9 @@
 // fixed-point results, and therefore the rounded binary64 values, are identical.
 #include "trig.h"
 
+#include <algorithm>
 #include <cstring>
+#include <thread>
 
 namespace lfg {
 namespace {
@@ -127,6 +129,8 @@ void cos_sin_fixed(const Fx& theta, Fx* cos_out, Fx* sin_out) {
   for (uint64_t j = 1; j < 40; ++j) {
     tc = divs(fmul(tc, th2), (2 * j - 1) * (2 * j));
     ts = divs(fmul(ts, th2), (2 * j) * (2 * j + 1));
+    // once both terms are zero every later term is zero too: stopping adds nothing
+    if (is_zero(tc) && is_zero(ts)) break;
     if (j % 2 == 1) {
       c_neg = add(c_neg, tc);
       s_neg = add(s_neg, ts);
@@ -220,8 +224,21 @@ std::vector<double> cos_sin_2pi_table(uint64_t n) {
   std::vector<double> out(2 * n);
   if (n == 0) return out;
   uint64_t g = gcd64(8, n);
-  std::vector<double> memo(2 * (n / g + 1));
-  for (uint64_t i = 0; i <= n / g; ++i) small_at(n, g * i, &memo[2 * i], &memo[2 * i + 1]);
+  const uint64_t nm = n / g + 1;
+  std::vector<double> memo(2 * nm);
+  // the series of different angles are independent: spread large tables over host threads
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = nm < 4096 ? 1 : std::max(1u, std::min(nt, 32u));
+  auto work = [&](unsigned id) {
+    for (uint64_t i = id; i < nm; i += nt) small_at(n, g * i, &memo[2 * i], &memo[2 * i + 1]);
+  };
+  if (nt == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t) pool.emplace_back(work, t);
+    for (auto& th : pool) th.join();
+  }
   auto lookup = [&](uint64_t num, double* cc, double* ss) {
     *cc = memo[2 * (num / g)];
     *ss = memo[2 * (num / g) + 1];

@@ -7,6 +7,7 @@ interface (`plan`), the torch integration and the codelet generator used at buil
 """
 from ._lib import LfgError, Unsupported, lib  # noqa: F401
 from .plan import Plan, cos_sin_table, plan_1d, plan_measure, plan_spec  # noqa: F401
+from .ragged import RaggedPlan, plan_ragged, ragged_sizes  # noqa: F401
 
 __all__ = ["Plan", "plan_1d", "plan_measure", "plan_spec", "cos_sin_table", "LfgError",
-           "Unsupported", "lib"]
+           "Unsupported", "lib", "RaggedPlan", "plan_ragged", "ragged_sizes"]

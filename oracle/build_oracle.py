@@ -25,7 +25,7 @@ BUILD = os.path.join(HERE, "_build")
 
 # Radices for which C codelets are generated (every GPU radix and a few larger ones
 # used by the reference's own published plans).
-ORACLE_RADICES = [2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 18, 20, 24, 25, 27, 32, 64]
+ORACLE_RADICES = [2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 18, 20, 24, 25, 27, 32, 36, 64]
 
 
 def build(force: bool = False) -> str:
@@ -35,16 +35,18 @@ def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     so = os.path.join(BUILD, "liboracle.so")
     src = os.path.join(HERE, "refstock.c")
+    trig = os.path.join(HERE, "trig_ref.c")
     cod = os.path.join(BUILD, "codelets_ref.c")
     text = c_codelets(ORACLE_RADICES)
     if not os.path.exists(cod) or open(cod).read() != text:
         with open(cod, "w") as f:
             f.write(text)
     if (not force and os.path.exists(so)
-            and os.path.getmtime(so) >= max(os.path.getmtime(src), os.path.getmtime(cod))):
+            and os.path.getmtime(so) >= max(os.path.getmtime(src), os.path.getmtime(cod),
+                                        os.path.getmtime(trig))):
         return so
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
-           "-std=gnu11", "-o", so + ".tmp", src, cod, "-lm"]
+           "-std=gnu11", "-o", so + ".tmp", src, trig, cod, "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(so + ".tmp", so)
     return so

@@ -55,8 +55,16 @@ def lib() -> ctypes.CDLL:
     L.lfo_dd_dft.argtypes = [ctypes.c_int, ctypes.c_long, _dp, _dp, ctypes.c_long, ctypes.c_long,
                              _dp, _dp, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_int]
     L.lfo_dd_dft.restype = ctypes.c_int
+    L.lfo_ref_ragged.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.POINTER(ctypes.c_long),
+                                 ctypes.POINTER(ctypes.c_int), ctypes.c_void_p, ctypes.c_void_p,
+                                 ctypes.c_long, ctypes.POINTER(ctypes.c_long),
+                                 ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long),
+                                 _dp, _dp, ctypes.c_int]
+    L.lfo_ref_ragged.restype = ctypes.c_int
     L.lfo_rel_l2.argtypes = [_dp, _dp, _dp, ctypes.c_long]
     L.lfo_rel_l2.restype = ctypes.c_double
+    L.lfo_cos_sin_table.argtypes = [ctypes.c_uint64, _dp]
+    L.lfo_cos_sin_table.restype = ctypes.c_int
     return L
 
 
@@ -79,13 +87,36 @@ def pass_ns(rs: Sequence[int], t: int) -> int:
     return p
 
 
-@lru_cache(maxsize=64)
+@lru_cache(maxsize=4096)
+def table(n: int) -> np.ndarray:
+    """cosSin2PiTable n (Trig.lean:131-134) as an (n, 2) array, from the oracle's C
+    restatement (trig_ref.c; checked against trig_ref.py in the tests)."""
+    out = np.empty(2 * n, dtype=np.float64)
+    assert lib().lfo_cos_sin_table(n, _p(out)) == 0
+    return out.reshape(n, 2)
+
+
+def pass_twiddles(tab: np.ndarray, fwd: bool, N: int, R: int, ns: int) -> np.ndarray:
+    """FastPlan.lean:163-173 on a table array: for r = 1..R-1 the ns real parts then the ns
+    imaginary parts of tab[r*k*N/(ns*R)], imaginary negated (never to -0.0) when fwd."""
+    step = N // (ns * R)
+    k = np.arange(ns)
+    rows = []
+    for r in range(1, R):
+        t = tab[r * k * step]
+        im = t[:, 1]
+        if fwd:
+            im = np.where(im == 0.0, 0.0, -im)
+        rows += [t[:, 0], im]
+    return np.ascontiguousarray(np.concatenate(rows)) if rows else np.zeros(0)
+
+
+@lru_cache(maxsize=4096)
 def _plan_twiddles(fwd: bool, N: int, rs: tuple):
-    tab = trig_ref.table(N)
+    tab = table(N)
     out = [np.zeros(1)]
     for t in range(1, len(rs)):
-        out.append(np.ascontiguousarray(
-            trig_ref.pass_twiddles(tab, fwd, N, rs[t], pass_ns(rs, t)), dtype=np.float64))
+        out.append(pass_twiddles(tab, fwd, N, rs[t], pass_ns(rs, t)))
     return out
 
 
@@ -94,9 +125,8 @@ def plan_twiddles(fwd: bool, N: int, rs: Sequence[int]) -> List[np.ndarray]:
     return _plan_twiddles(bool(fwd), int(N), tuple(int(r) for r in rs))
 
 
-@lru_cache(maxsize=64)
 def _tab_array(n: int) -> np.ndarray:
-    return np.ascontiguousarray(np.array(trig_ref.table(n), dtype=np.float64).reshape(-1))
+    return table(n).reshape(-1)
 
 
 @lru_cache(maxsize=64)
@@ -128,6 +158,37 @@ def ref_transform(fwd: bool, N: int, rs: Sequence[int], x: np.ndarray,
                                  nthreads)
     assert rc == 0, "reference transform failed (radix without a codelet?)"
     return out.reshape(shape)
+
+
+class RaggedRef:
+    """refTransform over a ragged batch in one C call (one transform per thread): sizes[i]
+    with radices plans[sizes[i]], data at complex offsets in_off[i] / out_off[i]."""
+
+    def __init__(self, fwd: bool, sizes, plans, in_off, out_off):
+        self.fwd = bool(fwd)
+        classes = sorted(set(int(n) for n in sizes))
+        idx = {n: c for c, n in enumerate(classes)}
+        self.cN = (ctypes.c_long * len(classes))(*classes)
+        self.cnp = (ctypes.c_int * len(classes))(*[len(plans[n]) for n in classes])
+        self._rs = [(ctypes.c_int * len(plans[n]))(*plans[n]) for n in classes]
+        self.crs = (ctypes.POINTER(ctypes.c_int) * len(classes))(
+            *[ctypes.cast(a, ctypes.POINTER(ctypes.c_int)) for a in self._rs])
+        self._tw = [plan_twiddles(fwd, n, plans[n]) for n in classes]
+        self._twp = [(_dp * len(t))(*[_p(a) for a in t]) for t in self._tw]
+        self.ctw = (ctypes.POINTER(_dp) * len(classes))(
+            *[ctypes.cast(a, ctypes.POINTER(_dp)) for a in self._twp])
+        self.ncls = len(classes)
+        self.count = len(sizes)
+        self.cls = (ctypes.c_long * len(sizes))(*[idx[int(n)] for n in sizes])
+        self.ioff = (ctypes.c_long * len(sizes))(*[int(v) for v in in_off])
+        self.ooff = (ctypes.c_long * len(sizes))(*[int(v) for v in out_off])
+
+    def run(self, x: np.ndarray, out: np.ndarray, nthreads: int = 1) -> np.ndarray:
+        rc = lib().lfo_ref_ragged(int(self.fwd), self.ncls, self.cN, self.cnp, self.crs,
+                                  self.ctw, self.count, self.cls, self.ioff, self.ooff,
+                                  _p(x.view(np.float64)), _p(out.view(np.float64)), nthreads)
+        assert rc == 0
+        return out
 
 
 def generic_dft(fwd: bool, x: np.ndarray, nthreads: int = 1) -> np.ndarray:

@@ -90,6 +90,39 @@ int lfo_ref_transform(int fwd, long N, const int *rs, int npass, const double *c
      return err ? -1 : 0;
 }
 
+/* refTransform over a ragged batch: transform i has class cls[i] (size cN[c], radices
+ * crs[c][0..cnp[c]), pass tables ctw[c][t]) and lives at complex offsets ioff[i] / ooff[i].
+ * One transform per thread. */
+int lfo_ref_ragged(int fwd, long ncls, const long *cN, const int *cnp, const int *const *crs,
+                   const double *const *const *ctw, long count, const long *cls,
+                   const long *ioff, const long *ooff, const double *in, double *out,
+                   int nthreads)
+{
+     int err = 0;
+     long i;
+     (void) ncls;
+     if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4) reduction(| : err)
+     for (i = 0; i < count; ++i) {
+          long c = cls[i], N = cN[c];
+          double *w0 = (double *) malloc(sizeof(double) * 4 * (size_t) N);
+          double *a = w0, *bb = w0 + 2 * N;
+          long ns = 1;
+          int t;
+          if (!w0) { err |= 1; continue; }
+          memcpy(a, in + 2 * ioff[i], sizeof(double) * 2 * (size_t) N);
+          for (t = 0; t < cnp[c]; ++t) {
+               double *tmp;
+               err |= ref_pass(fwd, N, crs[c][t], ns, t >= 1 ? ctw[c][t] : NULL, a, bb) != 0;
+               tmp = a; a = bb; bb = tmp;
+               ns *= crs[c][t];
+          }
+          memcpy(out + 2 * ooff[i], a, sizeof(double) * 2 * (size_t) N);
+          free(w0);
+     }
+     return err ? -1 : 0;
+}
+
 /* ------------------------------------------------------------------ 2. generic engine */
 
 /* Textbook product with four rounded products (FloatOps.lean:52-53). */

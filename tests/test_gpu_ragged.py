@@ -1,0 +1,95 @@
+"""GPU parity of ragged batches (one persistent, graph-replayed launch for many sizes).
+
+Every transform of the batch must equal the oracle's refTransform for its size and the
+radix sequence the plan picked, bit for bit, in every execution mode (persistent kernel
+with and without graph replay, per-size launches), with scattered offsets whose gaps stay
+untouched.  The full benchmark batch (8192 sizes drawn log-uniformly from the 13-smooth
+integers in [2, 16384]) is checked completely.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no GPU", allow_module_level=True)
+
+import lfg  # noqa: E402
+import oracle as O  # noqa: E402
+
+SENT = complex(-7.5e300, 3.25e299)
+
+
+def _check(plan, sizes, x, y_np, in_off, out_off):
+    bad = []
+    by_size = {}
+    for i, n in enumerate(sizes):
+        by_size.setdefault(int(n), []).append(i)
+    for n, idx in by_size.items():
+        rs = plan.radices(n)
+        xs = np.stack([x[in_off[i]: in_off[i] + n] for i in idx])
+        ref = O.ref_transform(True, n, rs, xs, nthreads=8)
+        got = np.stack([y_np[out_off[i]: out_off[i] + n] for i in idx])
+        if not np.array_equal(got.view(np.uint64), ref.view(np.uint64)):
+            bad.append((n, rs))
+    return bad
+
+
+@pytest.mark.parametrize("mode", ["graph", "direct", "per_size"])
+def test_ragged_small_scattered(mode):
+    rng = np.random.default_rng(3)
+    sizes = np.array([2, 3, 16, 60, 60, 60, 1000, 4096, 2310, 7, 13, 13, 8192, 10368, 16384,
+                      15015, 243, 2, 1024, 1024] * 2, dtype=np.int64)
+    rng.shuffle(sizes)
+    gaps = rng.integers(0, 5, size=sizes.size)
+    in_off = np.cumsum(np.concatenate([[3], sizes[:-1] + gaps[:-1]])).astype(np.int64)
+    out_off = np.cumsum(np.concatenate([[1], sizes[:-1] + gaps[::-1][:-1]])).astype(np.int64)
+    tin = int(in_off[-1] + sizes[-1] + 2)
+    tout = int(out_off[-1] + sizes[-1] + 7)
+    x = O.uniform_complex((tin,), seed=9)
+    plan = lfg.plan_ragged(sizes, -1, in_off, out_off, per_size=(mode == "per_size"),
+                           graph=(mode != "direct"))
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.full((tout,), SENT, dtype=torch.complex128, device="cuda")
+    for _ in range(2):        # a second execution reuses the graph and the zeroed queue
+        plan.execute(xd, yd)
+    torch.cuda.synchronize()
+    y = yd.cpu().numpy()
+    assert not _check(plan, sizes, x, y, in_off, out_off)
+    mask = np.ones(tout, bool)
+    for o, n in zip(out_off, sizes):
+        mask[o: o + n] = False
+    assert np.all(y[mask] == SENT)
+
+
+def test_ragged_benchmark_batch_full():
+    sizes = lfg.ragged_sizes(8192)
+    plan = lfg.plan_ragged(sizes, -1)
+    info = plan.info()
+    assert info.count == 8192 and info.launches == 1
+    total = int(sizes.sum())
+    x = O.uniform_complex((total,), seed=20261016)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    plan.execute(xd, yd)
+    torch.cuda.synchronize()
+    y = yd.cpu().numpy()
+    assert not _check(plan, sizes, x, y, plan.in_offsets, plan.out_offsets)
+    # per-size strategy gives the same bits
+    ps = lfg.plan_ragged(sizes, -1, per_size=True)
+    y2 = torch.empty_like(xd)
+    ps.execute(xd, y2)
+    torch.cuda.synchronize()
+    assert torch.equal(y2.view(torch.float64), yd.view(torch.float64))
+
+
+def test_ragged_host_entry():
+    sizes = np.array([12, 5000, 3, 720], dtype=np.int64)
+    x = O.uniform_complex((int(sizes.sum()),), seed=1)
+    plan = lfg.plan_ragged(sizes, 1)
+    y = plan.execute_host(x, np.zeros_like(x))
+    off = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    for o, n in zip(off, sizes):
+        ref = O.ref_transform(False, int(n), plan.radices(int(n)), x[o: o + n])
+        assert np.array_equal(y[o: o + n].view(np.uint64), ref.view(np.uint64))
