@@ -65,9 +65,13 @@ def fp64_peak():
     return None
 
 
+PROFILE_OF = {"ragged": "ragged_kernel_f64_ragged8192.md",
+              "c2c_1024": "group_kernel_f64_c2c1024.md"}
+
+
 def ncu_traffic(workload):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", f"stockham_f64_{workload}.md")
+    p = os.path.join(ROOT, "profiles", PROFILE_OF.get(workload, "-"))
     if os.path.exists(p):
         for line in open(p):
             if line.startswith("traffic_bytes_per_launch:"):

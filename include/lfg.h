@@ -36,6 +36,7 @@ typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
 #define LFG_MEASURE 1u       /* time the leading candidates on the device, keep the fastest */
 #define LFG_PER_SIZE 2u      /* ragged: one launch per distinct size (the comparison point)  */
 #define LFG_NO_GRAPH 4u      /* ragged: launch directly instead of replaying a CUDA graph    */
+#define LFG_ADJOINT 8u       /* r2c/c2r: exact cotangent scaling of the adjoint (see below)  */
 
 typedef struct lfg_plan lfg_plan;
 
@@ -63,6 +64,30 @@ lfg_status lfg_plan_1d(size_t n, int sign, size_t howmany, lfg_precision precisi
  * (LeanFFTW/Gen/Stockham.lean:298-301).  Used by the autotuner and by parity tests. */
 lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision precision,
                                const int *radices, int npass, lfg_plan **out);
+
+/* Real-input forward (r2c) and real-output backward (c2r) transforms, even n (13-smooth),
+ * `howmany` contiguous lines: real lines of n doubles, complex lines of n/2+1 interleaved
+ * values.  The rank-2 versions transform n0 x n1 images (r2c along the last axis, then a
+ * complex DFT along the first; c2r the reverse), images contiguous.  Replaces the generic
+ * engine's rdft2 path (`planProblemCore`, LeanFFTW/Core/Problem.lean:222-236, and
+ * `LineOp.apply`, :142-150); c2r ignores the imaginary parts of the self-conjugate bins
+ * (docs/CONTRACT.md:20-23). */
+lfg_status lfg_plan_r2c(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
+                        lfg_plan **out);
+lfg_status lfg_plan_c2r(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
+                        lfg_plan **out);
+lfg_status lfg_plan_r2c_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
+                           unsigned flags, lfg_plan **out);
+lfg_status lfg_plan_c2r_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
+                           unsigned flags, lfg_plan **out);
+
+/* With LFG_ADJOINT, lfg_plan_r2c doubles its output bins 1..n/2-1 (the gradient of c2r) and
+ * lfg_plan_c2r halves its input bins 1..n/2-1 (the gradient of r2c), both exactly, inside
+ * the kernels: the adjoint of each transform is the other one with this cotangent scaling. */
+
+/* Multiply the outputs of a complex plan by `scale` in the kernel's store (1 = off, the
+ * default; normalised or orthonormal conventions and their adjoints). */
+lfg_status lfg_set_scale(lfg_plan *plan, double scale);
 
 /* Execute on device pointers, enqueued on `stream` (a cudaStream_t; NULL = legacy default
  * stream).  in == out is allowed.  Replaces `lfa_call(rec, in, out)`
@@ -119,6 +144,7 @@ typedef struct {
   const int64_t *over_n;
   const int *over_npass;
   const int *over_radices;
+  int block_shape;      /* persistent-kernel block shape 0..4 (threads x CTAs per SM)   */
 } lfg_ragged_tuning;
 
 lfg_status lfg_plan_ragged(const int64_t *sizes, size_t count, const int64_t *in_offsets,

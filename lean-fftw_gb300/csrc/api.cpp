@@ -82,6 +82,65 @@ lfg_status finish_c2c(lfg::Plan& p, lfg_plan** out) {
   return LFG_OK;
 }
 
+lfg_status finish_real(lfg::Plan& p, const lfg::RealLayout& L, lfg_plan** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  p.device = dev;
+  p.howmany = L.howmany;
+  p.n = L.n;
+  const int64_t M = L.n / 2;
+  // spans: real side in doubles, complex side in doubles (2 per element)
+  const int64_t rspan = L.r_off + (L.howmany - 1) * L.r_bdist + (L.n0 - 1) * L.r_rdist + L.n;
+  const int64_t cspan = 2 * (L.c_off + (L.howmany - 1) * L.c_bdist + (L.n0 - 1) * L.c_rdist + M + 1);
+  const bool r2c = p.kind == lfg::Kind::R2C;
+  p.in_span = r2c ? rspan : cspan;
+  p.out_span = r2c ? cspan : rspan;
+  if (!p.empty) {
+    if ((e = lfg::prepare_group_kernels_f64()) != cudaSuccess) return cuda_fail(e, "kernel set-up");
+    if ((e = lfg::prepare_real_kernels_f64()) != cudaSuccess) return cuda_fail(e, "kernel set-up");
+    std::string msg = lfg::build_real(p, L, tile_target());
+    if (!msg.empty()) {
+      lfg::free_plan_memory(p);
+      return fail(LFG_ERR_UNSUPPORTED, msg);
+    }
+  }
+  lfg_plan* h = new (std::nothrow) lfg_plan;
+  if (!h) {
+    lfg::free_plan_memory(p);
+    return fail(LFG_ERR_NOMEM, "host allocation");
+  }
+  h->p = p;
+  *out = h;
+  return LFG_OK;
+}
+
+lfg_status plan_real_common(bool r2c, size_t n0, size_t n, size_t howmany, lfg_precision precision,
+                            unsigned flags, lfg_plan** out) {
+  if (!out) return fail(LFG_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (precision != LFG_F64) return fail(LFG_ERR_UNSUPPORTED, "precision not supported yet");
+  if (n < 2 || n0 < 1) return fail(LFG_ERR_UNSUPPORTED, "sizes must be >= 2 (last) and >= 1");
+  if (!smooth13((int64_t)n) || !smooth13((int64_t)n0))
+    return fail(LFG_ERR_UNSUPPORTED, "sizes must be 13-smooth");
+  lfg::Plan p;
+  p.kind = r2c ? lfg::Kind::R2C : lfg::Kind::C2R;
+  p.precision = precision;
+  p.fwd = r2c;
+  p.empty = howmany == 0;
+  lfg::RealLayout L;
+  L.n0 = (int64_t)n0;
+  L.n = (int64_t)n;
+  L.howmany = std::max<int64_t>(1, (int64_t)howmany);
+  L.r_rdist = (int64_t)n;
+  L.r_bdist = (int64_t)(n0 * n);
+  L.c_rdist = (int64_t)(n / 2 + 1);
+  L.c_bdist = (int64_t)(n0 * (n / 2 + 1));
+  if ((flags & LFG_ADJOINT) && n0 > 1) return fail(LFG_ERR_UNSUPPORTED, "adjoint scaling is 1-D only");
+  p.real.adjoint = (flags & LFG_ADJOINT) ? 1 : 0;
+  return finish_real(p, L, out);
+}
+
 lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision precision,
                           const int* radices, int npass, lfg_plan** out) {
   if (!out) return fail(LFG_ERR_INVALID, "null output handle");
@@ -118,6 +177,26 @@ lfg_status lfg_plan_1d(size_t n, int sign, size_t howmany, lfg_precision precisi
   return plan_1d_common(n, sign, howmany, precision, nullptr, 0, out);
 }
 
+lfg_status lfg_plan_r2c(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
+                        lfg_plan** out) {
+  return plan_real_common(true, 1, n, howmany, precision, flags, out);
+}
+
+lfg_status lfg_plan_c2r(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
+                        lfg_plan** out) {
+  return plan_real_common(false, 1, n, howmany, precision, flags, out);
+}
+
+lfg_status lfg_plan_r2c_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
+                           unsigned flags, lfg_plan** out) {
+  return plan_real_common(true, n0, n1, howmany, precision, flags, out);
+}
+
+lfg_status lfg_plan_c2r_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
+                           unsigned flags, lfg_plan** out) {
+  return plan_real_common(false, n0, n1, howmany, precision, flags, out);
+}
+
 lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision precision,
                                const int* radices, int npass, lfg_plan** out) {
   if (!radices) return fail(LFG_ERR_INVALID, "null radices");
@@ -148,7 +227,54 @@ lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precisi
     *os = (int64_t)spec[10 + 3 * i];
   };
   if (precision != LFG_F64) return fail(LFG_ERR_UNSUPPORTED, "precision not supported yet");
-  if (kind != 0) return fail(LFG_ERR_UNSUPPORTED, "only complex DFTs (kind 0) are executed so far");
+  if (kind == 1) {
+    // rdft2 (Core/Problem.lean:222-236): r2c when sign < 0 (real input), else c2r; the last
+    // dimension is halved on the complex side.  Executed: rank 1 or 2, vector rank <= 1, unit
+    // stride along the last axis on both sides, interleaved complex side.
+    if (rank < 1 || rank > 2 || vrank > 1)
+      return fail(LFG_ERR_UNSUPPORTED, "rdft2: rank 1-2 and vector rank <= 1 are executed");
+    const bool r2c = sign < 0;
+    const int64_t rRe = r2c ? inRe : outRe;
+    const int64_t cRe = r2c ? outRe : inRe, cIm = r2c ? outIm : inIm;
+    if (cIm != cRe + 1 || (cRe & 1) || rRe < 0 || cRe < 0)
+      return fail(LFG_ERR_UNSUPPORTED, "rdft2: the complex side must be interleaved");
+    lfg::RealLayout L;
+    int64_t nl, isl, osl;
+    dim(rank - 1, &nl, &isl, &osl);
+    const int64_t rstl = r2c ? isl : osl, cstl = r2c ? osl : isl;
+    if (rstl != 1 || cstl != 2)
+      return fail(LFG_ERR_UNSUPPORTED, "rdft2: unit stride along the last axis is required");
+    L.n = nl;
+    if (rank == 2) {
+      int64_t n0, is0, os0;
+      dim(0, &n0, &is0, &os0);
+      L.n0 = n0;
+      L.r_rdist = r2c ? is0 : os0;
+      const int64_t cr = r2c ? os0 : is0;
+      if (cr & 1) return fail(LFG_ERR_UNSUPPORTED, "rdft2: complex row pitch must be whole elements");
+      L.c_rdist = cr / 2;
+    }
+    int64_t vn = 1, vis = 0, vos = 0;
+    if (vrank == 1) dim(rank, &vn, &vis, &vos);
+    if (vn < 0) return fail(LFG_ERR_INVALID, "negative vector dimension");
+    L.howmany = vn;
+    L.r_bdist = r2c ? vis : vos;
+    const int64_t cb = r2c ? vos : vis;
+    if (cb & 1) return fail(LFG_ERR_UNSUPPORTED, "rdft2: complex vector pitch must be whole elements");
+    L.c_bdist = cb / 2;
+    L.r_off = rRe;
+    L.c_off = cRe / 2;
+    if (L.n < 2 || !smooth13(L.n) || !smooth13(L.n0))
+      return fail(LFG_ERR_UNSUPPORTED, "rdft2: sizes must be 13-smooth");
+    lfg::Plan p;
+    p.kind = r2c ? lfg::Kind::R2C : lfg::Kind::C2R;
+    p.precision = precision;
+    p.fwd = r2c;
+    p.empty = vn == 0;
+    if (p.empty) L.howmany = 1;
+    return finish_real(p, L, out);
+  }
+  if (kind != 0) return fail(LFG_ERR_UNSUPPORTED, "r2r (kind 2) is not executed on the GPU");
   for (int64_t d = 0; d < rank; ++d) {
     int64_t n, is, os;
     dim(d, &n, &is, &os);
@@ -211,7 +337,9 @@ lfg_status lfg_execute_host(const lfg_plan* plan, const void* in, void* out) {
   void* dout = inplace ? p.d_host_in : p.d_host_out;
   if ((e = cudaMemcpy(din, in, ib, cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_fail(e, "host-to-device copy");
-  if (!inplace && (e = cudaMemcpy(dout, out, ob, cudaMemcpyHostToDevice)) != cudaSuccess)
+  // an output span with gaps keeps the caller's values there: bring them along
+  const bool dense = p.out.offset == 0 && p.out.stride == 1 && (p.howmany == 1 || p.out.dist == p.n);
+  if (!inplace && !dense && (e = cudaMemcpy(dout, out, ob, cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_fail(e, "host-to-device copy");
   if ((e = lfg::execute_plan(p, din, dout, 0)) != cudaSuccess) return cuda_fail(e, "execute");
   if ((e = cudaMemcpy(out, dout, ob, cudaMemcpyDeviceToHost)) != cudaSuccess)
@@ -223,6 +351,15 @@ void lfg_destroy(lfg_plan* plan) {
   if (!plan) return;
   lfg::free_plan_memory(plan->p);
   delete plan;
+}
+
+lfg_status lfg_set_scale(lfg_plan* plan, double scale) {
+  if (!plan) return fail(LFG_ERR_INVALID, "null plan");
+  if (!std::isfinite(scale)) return fail(LFG_ERR_INVALID, "scale must be finite");
+  lfg::Plan& p = plan->p;
+  if (p.kind != lfg::Kind::C2C) return fail(LFG_ERR_UNSUPPORTED, "scaling applies to complex plans");
+  if (p.ngroups >= 1) p.groups[p.ngroups - 1].scale = scale;
+  return LFG_OK;
 }
 
 lfg_status lfg_get_plan_info(const lfg_plan* plan, lfg_plan_info* info) {
@@ -272,11 +409,27 @@ lfg_status lfg_plan_ragged(const int64_t* sizes, size_t count, const int64_t* in
     acc_in += n;
     acc_out += n;
   }
+  {
+    // the outputs tile [0, out_span) exactly when sorted offsets leave no gap
+    std::vector<std::pair<int64_t, int64_t>> iv;
+    for (size_t i = 0; i < count; ++i) iv.push_back({r.out_off[i], sizes[i]});
+    std::sort(iv.begin(), iv.end());
+    int64_t pos = 0;
+    bool dense = true;
+    for (auto& q : iv) {
+      if (q.first != pos) { dense = false; break; }
+      pos += q.second;
+    }
+    r.out_dense = dense && pos == r.out_span;
+  }
   lfg::RaggedOptions opt;
   opt.tile_target = tile_target();
   if (tuning) {
     if (tuning->tile_target >= 16) opt.tile_target = tuning->tile_target;
     if (tuning->single_max >= 2) opt.single_max = tuning->single_max;
+    if (tuning->block_shape < 0 || tuning->block_shape >= lfg::kRaggedVariants)
+      return fail(LFG_ERR_INVALID, "bad block shape");
+    opt.variant = tuning->block_shape;
     for (int j = 0; j < tuning->n_over; ++j) {
       const int np = tuning->over_npass[j];
       if (np < 1 || np > lfg::kMaxPass) return fail(LFG_ERR_INVALID, "bad override pass count");
@@ -333,7 +486,8 @@ lfg_status lfg_execute_ragged_host(const lfg_ragged* plan, const void* in, void*
   }
   if ((e = cudaMemcpy(r.d_host_in, in, ib, cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_fail(e, "host-to-device copy");
-  if ((e = cudaMemcpy(r.d_host_out, out, ob, cudaMemcpyHostToDevice)) != cudaSuccess)
+  // an output span with gaps keeps the caller's values there: bring them along
+  if (!r.out_dense && (e = cudaMemcpy(r.d_host_out, out, ob, cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_fail(e, "host-to-device copy");
   if ((e = lfg::execute_ragged(r, r.d_host_in, r.d_host_out, 0)) != cudaSuccess)
     return cuda_fail(e, "execute ragged");

@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "real.h"
 #include "stockham.h"
 
 namespace lfg {
@@ -42,7 +43,26 @@ struct Plan {
   mutable void* d_host_in = nullptr;     // staging buffers of lfg_execute_host
   mutable void* d_host_out = nullptr;
   bool empty = false;    // a vector dimension of size 0: nothing to do
+  // real transforms (kind R2C / C2R): rows of the last dimension, and for rank 2 the complex
+  // transform along the first dimension (columns of the half spectrum)
+  RealDesc real{};
+  bool has_col = false;
+  GroupDesc col{};
+  int64_t col_in_off = 0;        // c2r rank 2: complex offset of the input's first element
+  void* d_post = nullptr;
+  void* d_col_twiddles = nullptr;
 };
+
+// Geometry of a real transform: vector count `howmany`, rank-2 size n0 x n (rank 1: n0 = 1).
+// Real side in doubles, complex side in complex elements; unit stride along the last axis.
+struct RealLayout {
+  int64_t n0 = 1, n = 0, howmany = 1;
+  int64_t r_off = 0, r_bdist = 0, r_rdist = 0;
+  int64_t c_off = 0, c_bdist = 0, c_rdist = 0;
+};
+
+// Build a real plan (p.kind R2C or C2R, p.fwd set accordingly).  Returns "" on success.
+std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target);
 
 // Radix sequence with the fewest codelet operations for size n (first pass untwiddled),
 // or an empty vector when n is not 13-smooth.

@@ -14,6 +14,7 @@
 #include "generated/opcounts.h"
 #include "kernels.h"
 #include "plan.h"
+#include "real.h"
 #include "trig.h"
 
 namespace lfg {
@@ -107,7 +108,10 @@ void free_plan_memory(Plan& p) {
   if (p.d_scratch) cudaFree(p.d_scratch);
   if (p.d_host_in) cudaFree(p.d_host_in);
   if (p.d_host_out) cudaFree(p.d_host_out);
+  if (p.d_post) cudaFree(p.d_post);
+  if (p.d_col_twiddles) cudaFree(p.d_col_twiddles);
   p.d_twiddles = p.d_scratch = p.d_host_in = p.d_host_out = nullptr;
+  p.d_post = p.d_col_twiddles = nullptr;
   if (cur != p.device) cudaSetDevice(cur);
 }
 
@@ -162,6 +166,7 @@ void fill_group(GroupDesc& g, const std::vector<int>& rs, const PassTables& pt, 
   for (int t = 0; t < t0; ++t) P0 *= rs[t];
   g.kmul = (int)P0;
   g.twsub = t0 > 0 ? 1 : 0;
+  g.scale = 1.0;
   for (int t = t0; t < t1; ++t) {
     PassDesc& d = g.pass[t - t0];
     d.R = rs[t];
@@ -276,8 +281,123 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   return "";
 }
 
+std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
+  const int prec = p.precision;
+  const bool r2c = p.kind == Kind::R2C;
+  const int64_t N = L.n, M = N / 2;
+  if (N < 2 || (N & 1)) return "real transforms of odd size are not executed on the GPU";
+  if ((L.r_off & 1) || (L.r_bdist & 1) || (L.r_rdist & 1))
+    return "real lines must start at even double offsets";
+  const int64_t max_m = max_single_group(prec);
+  if (M > max_m) return "real transform too large for one pass group";
+  p.n = N;
+  RealDesc& d = p.real;
+  d.M = (int)M;
+  d.rows = L.n0;
+  d.lines = L.howmany * L.n0;
+  d.r_off = L.r_off;
+  d.r_bdist = L.r_bdist;
+  d.r_rdist = L.r_rdist;
+  d.c_off = L.c_off;
+  d.c_bdist = L.c_bdist;
+  d.c_rdist = L.c_rdist;
+  std::string msg;
+  // size-M passes (none for M = 1)
+  p.radices = M >= 2 ? choose_radices(M, prec) : std::vector<int>{};
+  PassTables pt;
+  if (M >= 2) {
+    msg = check_radices(M, p.radices);
+    if (!msg.empty()) return msg;
+    pt = make_pass_tables(M, r2c, p.radices, prec);
+  }
+  p.d_twiddles = upload_tables(pt.values, prec, &msg);
+  if (!p.d_twiddles) return msg;
+  if (M >= 2) {
+    fill_group(d.g, p.radices, pt, 0, (int)p.radices.size(), 1, tile_target, prec, p.d_twiddles);
+  } else {
+    d.g.M = 1;
+    d.g.npass = 0;
+    d.g.nsub = 1;
+    d.g.scale = 1.0;
+  }
+  int64_t cmax = std::max<int64_t>(1, tile_target / std::max<int64_t>(M, 1));
+  while (cmax > 1 && smem_bytes(cmax, M, prec) > kSmemBudget) --cmax;
+  d.g.C = (int)std::min<int64_t>(cmax, std::max<int64_t>(1, d.lines));
+  // split twiddles cos/sin(2 pi k / N), k = 0..M/2, halved for r2c
+  std::vector<double> tab = cos_sin_2pi_table((uint64_t)N);
+  // [halved table | full table]
+  const int64_t np = M / 2 + 1;
+  std::vector<double> post(4 * np);
+  for (int64_t k = 0; k < np; ++k) {
+    post[2 * k] = r2c ? 0.5 * tab[2 * k] : tab[2 * k];
+    post[2 * k + 1] = r2c ? 0.5 * tab[2 * k + 1] : tab[2 * k + 1];
+    post[2 * np + 2 * k] = tab[2 * k];
+    post[2 * np + 2 * k + 1] = tab[2 * k + 1];
+  }
+  p.d_post = upload_tables(post, prec, &msg);
+  if (!p.d_post) return msg;
+  d.post = p.d_post;
+  d.post_full = (const double*)p.d_post + 2 * np;
+  p.flops = (plan_ops(M, p.radices) + 6.0 * M) * (double)d.lines;
+  // rank 2: complex transform of length n0 along the first axis of the half spectrum
+  p.has_col = L.n0 > 1;
+  if (p.has_col) {
+    std::vector<int> crs = choose_radices(L.n0, prec);
+    msg = check_radices(L.n0, crs);
+    if (!msg.empty()) return msg;
+    if (L.n0 > max_m) return "first dimension too large for one pass group";
+    PassTables ct = make_pass_tables(L.n0, r2c, crs, prec);
+    p.d_col_twiddles = upload_tables(ct.values, prec, &msg);
+    if (!p.d_col_twiddles) return msg;
+    const int64_t h = M + 1;
+    GroupDesc& g = p.col;
+    fill_group(g, crs, ct, 0, (int)crs.size(), 1, tile_target, prec, p.d_col_twiddles);
+    int64_t cm = std::max<int64_t>(1, tile_target / L.n0);
+    while (cm > 1 && smem_bytes(cm, L.n0, prec) > kSmemBudget) --cm;
+    // columns of one image are the sub-problems; tiles may straddle images (no sub-problem
+    // index enters the twiddles of a single group)
+    g.nsub = (int)h;
+    g.total_sub = L.howmany * h;
+    g.C = (int)std::min<int64_t>(cm, g.total_sub);
+    g.in_sub = g.out_sub = 1;
+    if (r2c) {   // in place on the output
+      g.in_line = g.out_line = L.c_bdist;
+      g.in_elem = g.out_elem = L.c_rdist;
+    } else {     // from the input to a contiguous scratch image, then rows from the scratch
+      g.in_line = L.c_bdist;
+      g.in_elem = L.c_rdist;
+      g.out_line = L.n0 * h;
+      g.out_elem = h;
+      p.col_in_off = L.c_off;
+      d.c_off = 0;
+      // the column transform's output, allocated with the plan
+      const size_t need = (size_t)L.howmany * L.n0 * h * 16;
+      if (cudaMalloc(&p.d_scratch, need) != cudaSuccess) return "cudaMalloc of the c2r scratch failed";
+      p.scratch_bytes = need;
+      d.c_bdist = L.n0 * h;
+      d.c_rdist = h;
+    }
+    p.flops += plan_ops(L.n0, crs) * (double)(L.howmany * h);
+  }
+  return "";
+}
+
 cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream) {
   if (p.empty) return cudaSuccess;
+  if (p.kind == Kind::R2C) {
+    cudaError_t e = launch_real_f64(p.real, true, in, out, stream);
+    if (e != cudaSuccess || !p.has_col) return e;
+    const size_t es = 16;
+    char* ob = static_cast<char*>(out) + p.real.c_off * (int64_t)es;
+    return launch_group_f64(p.col, true, ob, ob, stream);
+  }
+  if (p.kind == Kind::C2R) {
+    if (!p.has_col) return launch_real_f64(p.real, false, in, out, stream);
+    const char* ib = static_cast<const char*>(in) + p.col_in_off * 16;
+    cudaError_t e = launch_group_f64(p.col, false, ib, p.d_scratch, stream);
+    if (e != cudaSuccess) return e;
+    return launch_real_f64(p.real, false, p.d_scratch, out, stream);
+  }
   const size_t es = p.precision == 0 ? 16 : 8;
   const char* ib = static_cast<const char*>(in) + p.in.offset * (int64_t)es;
   char* ob = static_cast<char*>(out) + p.out.offset * (int64_t)es;

@@ -177,7 +177,8 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
   r.launch.out_off = static_cast<const int64_t*>(r.d_out_off);
   r.launch.counter = static_cast<unsigned*>(r.d_counter);
   r.launch.smem = smem;
-  const int per_sm = prec == 0 ? ragged_blocks_per_sm_f64(smem) : 1;
+  r.launch.variant = opt.variant;
+  const int per_sm = prec == 0 ? ragged_blocks_per_sm_f64(smem, opt.variant) : 1;
   const int64_t want = (int64_t)prop.multiProcessorCount * per_sm;
   r.launch.grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)r.items_host.size()));
 

@@ -15,6 +15,7 @@ namespace lfg {
 struct RaggedOptions {
   int64_t tile_target = 2048;      // complex elements per CTA tile
   int64_t single_max = 2048;       // largest size run as one pass group
+  int variant = 0;                 // block shape of the persistent kernel
   std::map<int64_t, std::vector<int>> radices;   // per-size overrides (autotuner)
 };
 
@@ -41,6 +42,7 @@ struct RaggedPlan {
   std::vector<PerSizeLaunch> per_size;
   RaggedLaunch launch{};
   int64_t in_span = 0, out_span = 0;                   // complex elements
+  bool out_dense = false;                              // outputs tile [0, out_span) exactly
   double flops = 0;
   RaggedOptions options;
   void *d_twiddles = nullptr, *d_classes = nullptr, *d_items = nullptr, *d_in_off = nullptr,

@@ -51,6 +51,7 @@ struct GroupDesc {
   int64_t out_line, out_sub, out_elem;
   int kmul;              // table index k = k_loc * kmul + (twsub ? s % nsub : 0)
   int twsub;
+  double scale;          // outputs multiplied by this on store unless it is exactly 1
   PassDesc pass[kMaxPass];
 };
 
@@ -80,6 +81,7 @@ struct RaggedLaunch {
   unsigned int* counter;
   unsigned grid;
   size_t smem;
+  int variant;           // block shape of the persistent kernel (kernels.h)
 };
 
 }  // namespace lfg

@@ -37,8 +37,8 @@ group_kernel_f64(const GroupDesc g, const double2* in, double2* out) {
 // first group writes its intermediate to the output and whose second group then works on
 // the output in place; the barrier between them orders the global-memory traffic within
 // the CTA.  Items are sorted by decreasing cost, so the largest start first.
-template <bool FWD>
-__global__ void __launch_bounds__(kGroupThreads)
+template <bool FWD, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
 ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __restrict__ items,
                   int nitems, const int64_t* __restrict__ in_off,
                   const int64_t* __restrict__ out_off, const double2* in, double2* out,
@@ -83,20 +83,46 @@ size_t ragged_smem_bytes_f64(const RaggedClass& c) {
   return m;
 }
 
+// Block shapes of the persistent kernel the autotuner chooses from: (threads, minimum
+// resident CTAs per SM, which caps the registers per thread).
+using RaggedFn = void (*)(const RaggedClass*, const RaggedItem*, int, const int64_t*,
+                          const int64_t*, const double2*, double2*, unsigned int*);
+
+template <bool FWD>
+RaggedFn ragged_fn(int variant) {
+  switch (variant) {
+    case 1: return ragged_kernel_f64<FWD, 256, 1>;
+    case 2: return ragged_kernel_f64<FWD, 128, 2>;
+    case 3: return ragged_kernel_f64<FWD, 128, 3>;
+    case 4: return ragged_kernel_f64<FWD, 512, 1>;
+    default: return ragged_kernel_f64<FWD, 256, 2>;
+  }
+}
+
+int ragged_variant_threads(int variant) {
+  switch (variant) {
+    case 1: return 256;
+    case 2: return 128;
+    case 3: return 128;
+    case 4: return 512;
+    default: return 256;
+  }
+}
+
 cudaError_t launch_ragged_f64(const RaggedLaunch& r, bool fwd, const void* in, void* out,
                               cudaStream_t stream) {
   if (r.nitems <= 0) return cudaSuccess;
-  auto kern = fwd ? ragged_kernel_f64<true> : ragged_kernel_f64<false>;
-  kern<<<r.grid, kGroupThreads, r.smem, stream>>>(
+  RaggedFn kern = fwd ? ragged_fn<true>(r.variant) : ragged_fn<false>(r.variant);
+  kern<<<r.grid, ragged_variant_threads(r.variant), r.smem, stream>>>(
       r.classes, r.items, r.nitems, r.in_off, r.out_off, static_cast<const double2*>(in),
       static_cast<double2*>(out), r.counter);
   return cudaGetLastError();
 }
 
-int ragged_blocks_per_sm_f64(size_t smem) {
+int ragged_blocks_per_sm_f64(size_t smem, int variant) {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ragged_kernel_f64<true>, kGroupThreads,
-                                                    smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ragged_fn<true>(variant),
+                                                    ragged_variant_threads(variant), smem) != cudaSuccess)
     return 1;
   return nb > 0 ? nb : 1;
 }
@@ -117,8 +143,11 @@ cudaError_t prepare_group_kernels_f64() {
   cudaError_t e;
   if ((e = allow_max_smem(group_kernel_f64<true>)) != cudaSuccess) return e;
   if ((e = allow_max_smem(group_kernel_f64<false>)) != cudaSuccess) return e;
-  if ((e = allow_max_smem(ragged_kernel_f64<true>)) != cudaSuccess) return e;
-  return allow_max_smem(ragged_kernel_f64<false>);
+  for (int v = 0; v < kRaggedVariants; ++v) {
+    if ((e = allow_max_smem(ragged_fn<true>(v))) != cudaSuccess) return e;
+    if ((e = allow_max_smem(ragged_fn<false>(v))) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_group_f64(const GroupDesc& g, bool fwd, const void* in, void* out,

@@ -125,9 +125,31 @@ __device__ __forceinline__ void copy_tile(double2* tile, const double2* gin, dou
     const int64_t line = s / nsub;
     const int64_t sub = s - line * nsub;
     const int64_t a = (LOAD ? lines.in(line) : lines.out(line)) + sub * sub_st + (int64_t)i * elem_st;
-    if (LOAD) tile[c * M + i] = gin[a];
-    else gout[a] = tile[c * M + i];
+    if (LOAD) {
+      tile[c * M + i] = gin[a];
+    } else if (g.scale == 1.0) {
+      gout[a] = tile[c * M + i];
+    } else {
+      const double2 v = tile[c * M + i];
+      gout[a] = make_double2(__dmul_rn(v.x, g.scale), __dmul_rn(v.y, g.scale));
+    }
   }
+}
+
+// Run every pass of group g on a tile of C sub-problems held in shared-memory buffer A
+// (B is the ping-pong partner); returns the buffer holding the result.
+template <bool FWD>
+__device__ __forceinline__ double2* run_passes_f64(const GroupDesc& g, double2* A, double2* B,
+                                                   int C, int64_t msub0) {
+  const int npass = g.npass;
+  for (int t = 0; t < npass; ++t) {
+    run_pass_f64<FWD>(A, B, C, g.M, g.pass[t], g.kmul, msub0);
+    __syncthreads();
+    double2* tmp = A;
+    A = B;
+    B = tmp;
+  }
+  return A;
 }
 
 // Load C sub-problems starting at s0, run every pass of group g in shared memory, store.

@@ -25,6 +25,7 @@ LFG_F32 = 1
 
 LFG_ESTIMATE = 0
 LFG_MEASURE = 1
+LFG_ADJOINT = 8
 
 
 class PlanInfo(ctypes.Structure):
@@ -54,6 +55,15 @@ _SIG = {
     "lfg_plan_1d_radices": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t,
                                             ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                             ctypes.POINTER(_VP)]),
+    "lfg_plan_r2c": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint,
+                                     ctypes.POINTER(_VP)]),
+    "lfg_plan_c2r": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint,
+                                     ctypes.POINTER(_VP)]),
+    "lfg_plan_r2c_2d": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
+                                        ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_VP)]),
+    "lfg_plan_c2r_2d": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
+                                        ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_VP)]),
+    "lfg_set_scale": (ctypes.c_int, [_VP, ctypes.c_double]),
     "lfg_execute": (ctypes.c_int, [_VP, _VP, _VP, _VP]),
     "lfg_execute_host": (ctypes.c_int, [_VP, _VP, _VP]),
     "lfg_destroy": (None, [_VP]),

@@ -32,6 +32,11 @@ class Plan:
     def handle(self) -> int:
         return self._h.value
 
+    def set_scale(self, scale: float) -> "Plan":
+        """Multiply the outputs by `scale` inside the kernel (complex plans)."""
+        check(lib().lfg_set_scale(self._h, float(scale)))
+        return self
+
     def info(self) -> PlanInfo:
         pi = PlanInfo()
         check(lib().lfg_get_plan_info(self._h, ctypes.byref(pi)))
@@ -47,7 +52,7 @@ class Plan:
         addresses); the work is enqueued on `stream` (default: torch's current stream)."""
         import torch
         if out is None:
-            out = torch.empty_like(inp)
+            out = torch.empty_like(inp)   # complex transforms; real ones must pass `out`
         ip = inp.data_ptr() if hasattr(inp, "data_ptr") else int(inp)
         op = out.data_ptr() if hasattr(out, "data_ptr") else int(out)
         if stream is None:
@@ -98,6 +103,40 @@ def plan_1d(n: int, sign: int = -1, howmany: int = 1, precision="f64",
     else:
         check(lib().lfg_plan_1d(n, sign, howmany, _prec(precision),
                                 LFG_MEASURE if measure else LFG_ESTIMATE, ctypes.byref(h)))
+    return Plan(h)
+
+
+def plan_r2c(n: int, howmany: int = 1, precision="f64", adjoint: bool = False) -> Plan:
+    """Real forward transform of even size n on `howmany` contiguous lines: n doubles in,
+    n/2+1 complex out per line (the generic engine's r2c, Core/Problem.lean:145-147).
+    adjoint=True doubles output bins 1..n/2-1: the gradient of c2r."""
+    h = ctypes.c_void_p()
+    check(lib().lfg_plan_r2c(n, howmany, _prec(precision), _lib.LFG_ADJOINT if adjoint else 0,
+                             ctypes.byref(h)))
+    return Plan(h)
+
+
+def plan_c2r(n: int, howmany: int = 1, precision="f64", adjoint: bool = False) -> Plan:
+    """Backward transform of a half spectrum (n/2+1 complex per line) to n reals
+    (Core/Problem.lean:148-150): unnormalised, imaginary parts of bins 0 and n/2 ignored.
+    adjoint=True halves input bins 1..n/2-1: the gradient of r2c."""
+    h = ctypes.c_void_p()
+    check(lib().lfg_plan_c2r(n, howmany, _prec(precision), _lib.LFG_ADJOINT if adjoint else 0,
+                             ctypes.byref(h)))
+    return Plan(h)
+
+
+def plan_r2c_2d(n0: int, n1: int, howmany: int = 1, precision="f64") -> Plan:
+    """Rank-2 r2c of n0 x n1 real images to n0 x (n1/2+1) complex (Core/Problem.lean:228-233)."""
+    h = ctypes.c_void_p()
+    check(lib().lfg_plan_r2c_2d(n0, n1, howmany, _prec(precision), 0, ctypes.byref(h)))
+    return Plan(h)
+
+
+def plan_c2r_2d(n0: int, n1: int, howmany: int = 1, precision="f64") -> Plan:
+    """Rank-2 c2r: complex backward along the first axis, then c2r along the last."""
+    h = ctypes.c_void_p()
+    check(lib().lfg_plan_c2r_2d(n0, n1, howmany, _prec(precision), 0, ctypes.byref(h)))
     return Plan(h)
 
 

@@ -29,7 +29,7 @@ class RaggedTuning(ctypes.Structure):
     _fields_ = [("tile_target", ctypes.c_int64), ("single_max", ctypes.c_int64),
                 ("n_over", ctypes.c_int), ("over_n", ctypes.POINTER(ctypes.c_int64)),
                 ("over_npass", ctypes.POINTER(ctypes.c_int)),
-                ("over_radices", ctypes.POINTER(ctypes.c_int))]
+                ("over_radices", ctypes.POINTER(ctypes.c_int)), ("block_shape", ctypes.c_int)]
 
 
 _VP = ctypes.c_void_p
@@ -104,7 +104,7 @@ class RaggedPlan:
 
 def plan_ragged(sizes: Sequence[int], sign: int = -1, in_offsets=None, out_offsets=None,
                 per_size: bool = False, graph: bool = True, measure: bool = False,
-                tile_target: int = 0, single_max: int = 0,
+                tile_target: int = 0, single_max: int = 0, block_shape: int = 0,
                 radices: Optional[Dict[int, Sequence[int]]] = None) -> RaggedPlan:
     L = _bind()
     s = np.ascontiguousarray(sizes, dtype=np.int64)
@@ -112,7 +112,7 @@ def plan_ragged(sizes: Sequence[int], sign: int = -1, in_offsets=None, out_offse
     oo = None if out_offsets is None else np.ascontiguousarray(out_offsets, dtype=np.int64)
     flags = (LFG_PER_SIZE if per_size else 0) | (0 if graph else LFG_NO_GRAPH) | \
             (LFG_MEASURE if measure else 0)
-    tun = RaggedTuning(tile_target, single_max, 0, None, None, None)
+    tun = RaggedTuning(tile_target, single_max, 0, None, None, None, block_shape)
     keep = []
     if radices:
         ns = np.array(list(radices.keys()), dtype=np.int64)

@@ -1,0 +1,114 @@
+"""GPU r2c / c2r (rank 1 and 2) against the double-double oracle.
+
+lean-fftw computes these in its generic engine (Core/Problem.lean:142-150, 222-236); the
+parity bar is the relative L2 error against the extended-precision DFT: within 1.5x of the
+generic engine's own error (restated in the oracle) on the same inputs.  c2r must ignore the
+imaginary parts of bins 0 and n/2 (docs/CONTRACT.md:20-23).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no GPU", allow_module_level=True)
+
+import lfg  # noqa: E402
+import oracle as O  # noqa: E402
+
+SIZES = [2, 4, 6, 8, 10, 12, 16, 30, 60, 64, 210, 512, 1000, 1024, 2048, 4096, 8192, 10368]
+
+
+def _r2c(x, n):
+    B = x.shape[0]
+    plan = lfg.plan_r2c(n, B)
+    out = torch.empty((B, n // 2 + 1), dtype=torch.complex128, device="cuda")
+    plan.execute(torch.from_numpy(x).cuda(), out)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def _c2r(h, n):
+    B = h.shape[0]
+    plan = lfg.plan_c2r(n, B)
+    out = torch.empty((B, n), dtype=torch.float64, device="cuda")
+    plan.execute(torch.from_numpy(np.ascontiguousarray(h)).cuda(), out)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_r2c_error_vs_reference(n):
+    B = 4
+    x = np.random.default_rng(n).random((B, n)) - 0.5
+    ref = O.dd_r2c(x, nthreads=8)
+    e_gpu = O.rel_l2(_r2c(x, n), ref)
+    e_ref = O.rel_l2(O.generic_r2c(x, nthreads=8), ref)
+    assert e_gpu <= 1.5 * e_ref + 1e-17, (n, e_gpu, e_ref)
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_c2r_error_vs_reference(n):
+    B = 4
+    rng = np.random.default_rng(n + 1)
+    h = (rng.random((B, n // 2 + 1, 2)) - 0.5).view(np.complex128)[..., 0]
+    ref = O.dd_c2r(h, n, nthreads=8)
+    e_gpu = O.rel_l2(_c2r(h, n), ref)
+    e_ref = O.rel_l2(O.generic_c2r(h, n, nthreads=8), ref)
+    assert e_gpu <= 1.5 * e_ref + 1e-17, (n, e_gpu, e_ref)
+    # imaginary parts of the self-conjugate bins are ignored
+    h2 = h.copy()
+    h2[:, 0] += 3j
+    h2[:, n // 2] -= 5j
+    assert np.array_equal(_c2r(h2, n), _c2r(h, n))
+
+
+def test_r2c_c2r_pair_batch256_8192():
+    n, B = 8192, 256
+    x = np.random.default_rng(20261016).random((B, n)) - 0.5
+    X = _r2c(x, n)
+    e = O.rel_l2(X, O.dd_r2c(x, nthreads=16))
+    assert e < 4e-16, e
+    y = _c2r(X, n)
+    assert np.max(np.abs(y / n - x)) < 1e-14
+
+
+@pytest.mark.parametrize("n0,n1,B", [(512, 512, 3), (12, 60, 5), (64, 8, 2)])
+def test_rank2_r2c_c2r(n0, n1, B):
+    x = np.random.default_rng(7).random((B, n0, n1)) - 0.5
+    plan = lfg.plan_r2c_2d(n0, n1, B)
+    out = torch.empty((B, n0, n1 // 2 + 1), dtype=torch.complex128, device="cuda")
+    plan.execute(torch.from_numpy(x).cuda(), out)
+    torch.cuda.synchronize()
+    X = out.cpu().numpy()
+    ref = O.dd_rank2_r2c(x, nthreads=16)
+    e_gpu = O.rel_l2(X, ref)
+    e_gen = O.rel_l2(O.generic_rank2_r2c(x, nthreads=16), ref)
+    assert e_gpu <= 1.5 * e_gen + 1e-17, (e_gpu, e_gen)
+    back = lfg.plan_c2r_2d(n0, n1, B)
+    y = torch.empty((B, n0, n1), dtype=torch.float64, device="cuda")
+    xin = out.clone()
+    back.execute(out, y)
+    torch.cuda.synchronize()
+    assert torch.equal(xin, out)           # the input is not destroyed
+    assert np.max(np.abs(y.cpu().numpy() / (n0 * n1) - x)) < 1e-14
+
+
+def test_rdft2_spec_vector():
+    """FFI encoding of a batched r2c (kind 1, sign -1): real lines with a pitch, complex
+    output with a pitch (strides and offsets in doubles)."""
+    n, B = 360, 3
+    rpitch, cpitch = n + 6, n // 2 + 5          # doubles / complex elements
+    xbuf = np.random.default_rng(3).random(2 + rpitch * B) - 0.5
+    spec = [1, -1, 1, 1, 2, 2, 2, 3, n, 1, 2, B, rpitch, 2 * cpitch]
+    plan = lfg.plan_spec(spec)
+    out = torch.zeros(1 + cpitch * B, dtype=torch.complex128, device="cuda")
+    plan.execute(torch.from_numpy(xbuf).cuda(), out)
+    torch.cuda.synchronize()
+    o = out.cpu().numpy()
+    for b in range(B):
+        x = xbuf[2 + b * rpitch: 2 + b * rpitch + n]
+        got = o[1 + b * cpitch: 1 + b * cpitch + n // 2 + 1]
+        e = O.rel_l2(got, O.dd_r2c(x[None, :]))
+        assert e < 3e-16, e
