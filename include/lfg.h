@@ -37,6 +37,7 @@ typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
 #define LFG_PER_SIZE 2u      /* ragged: one launch per distinct size (the comparison point)  */
 #define LFG_NO_GRAPH 4u      /* ragged: launch directly instead of replaying a CUDA graph    */
 #define LFG_ADJOINT 8u       /* r2c/c2r: exact cotangent scaling of the adjoint (see below)  */
+#define LFG_NO_COMPENSATION 16u /* binary32: plain twiddle products in every pass             */
 
 typedef struct lfg_plan lfg_plan;
 

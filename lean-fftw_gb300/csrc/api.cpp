@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -13,6 +14,7 @@
 #include "plan.h"
 #include "ragged.h"
 #include "trig.h"
+#include "tuner.h"
 
 struct lfg_plan {
   lfg::Plan p;
@@ -51,20 +53,60 @@ int64_t tile_target() {
   return 2048;
 }
 
+int64_t single_max_default() {
+  const char* s = std::getenv("LFG_SINGLE_MAX");
+  if (s) {
+    long v = std::strtol(s, nullptr, 10);
+    if (v >= 2) return v;
+  }
+  return 2048;
+}
+
+// Device address of pinned (page-locked) host memory covering [p, p + bytes), or nullptr.
+// On GB300 the GPU reads and writes such memory over NVLink-C2C directly, so the host entry
+// points can stream the data through the kernels instead of copying it in and out first.
+void* mapped_device_ptr(const void* p, size_t bytes) {
+  if (!p || bytes == 0) return nullptr;
+  cudaPointerAttributes a, b;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const char* last = static_cast<const char*>(p) + bytes - 1;
+  if (cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer ||
+      !b.devicePointer)
+    return nullptr;
+  if (static_cast<const char*>(b.devicePointer) - static_cast<const char*>(a.devicePointer) !=
+      (ptrdiff_t)(bytes - 1))
+    return nullptr;
+  return a.devicePointer;
+}
+
 // Spanned scalars of a side: from the execution pointer to one past the last element.
-int64_t span_scalars(const lfg::Side& s, int64_t n, int64_t howmany, int per_elem) {
+int64_t span_scalars(const lfg::Side& s, int64_t n, int64_t howmany, int64_t per_elem) {
   return (s.offset + (n - 1) * s.stride + (howmany - 1) * s.dist + 1) * per_elem;
 }
 
 lfg_status finish_c2c(lfg::Plan& p, lfg_plan** out) {
+  // binary64 is bound by the FP64 pipe: two groups of small tiles (more CTAs per SM) beat one
+  // group with a CTA-sized tile above 2048 points; binary32 is bound by HBM: as few groups as fit
+  if (p.single_max == 0 && p.precision == 0) p.single_max = single_max_default();
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   p.device = dev;
   if (!p.empty) {
-    e = p.precision == 0 ? lfg::prepare_group_kernels_f64() : cudaErrorNotSupported;
+    e = p.precision == 0 ? lfg::prepare_group_kernels_f64() : lfg::prepare_group_kernels_f32();
     if (e != cudaSuccess) return cuda_fail(e, "kernel set-up");
-    std::string msg = lfg::build_c2c(p, tile_target());
+    if (p.measure) {
+      std::string msg = lfg::tune_c2c(p, tile_target());
+      if (!msg.empty()) return fail(LFG_ERR_CUDA, msg);
+    }
+    std::string msg = lfg::build_c2c(p, p.tile > 0 ? p.tile : tile_target());
     if (!msg.empty()) {
       lfg::free_plan_memory(p);
       return fail(LFG_ERR_UNSUPPORTED, msg);
@@ -142,11 +184,11 @@ lfg_status plan_real_common(bool r2c, size_t n0, size_t n, size_t howmany, lfg_p
 }
 
 lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision precision,
-                          const int* radices, int npass, lfg_plan** out) {
+                          const int* radices, int npass, lfg_plan** out, unsigned flags = 0) {
   if (!out) return fail(LFG_ERR_INVALID, "null output handle");
   *out = nullptr;
   if (sign != -1 && sign != 1) return fail(LFG_ERR_INVALID, "sign must be -1 or +1");
-  if (precision != LFG_F64) return fail(LFG_ERR_UNSUPPORTED, "precision not supported yet");
+  if (precision != LFG_F64 && precision != LFG_F32) return fail(LFG_ERR_INVALID, "bad precision");
   if (n < 2 || n > ((size_t)1 << 24)) return fail(LFG_ERR_UNSUPPORTED, "size outside 2..2^24");
   if (!smooth13((int64_t)n)) return fail(LFG_ERR_UNSUPPORTED, "size has a prime factor above 13");
   lfg::Plan p;
@@ -158,6 +200,8 @@ lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision prec
   p.in.stride = p.out.stride = 1;
   p.in.dist = p.out.dist = (int64_t)n;
   p.empty = howmany == 0;
+  p.no_comp = (flags & LFG_NO_COMPENSATION) != 0;
+  p.measure = (flags & LFG_MEASURE) != 0 && !radices;
   if (radices) {
     if (npass < 1 || npass > lfg::kMaxPass) return fail(LFG_ERR_INVALID, "bad pass count");
     p.radices.assign(radices, radices + npass);
@@ -173,8 +217,7 @@ extern "C" {
 
 lfg_status lfg_plan_1d(size_t n, int sign, size_t howmany, lfg_precision precision,
                        unsigned flags, lfg_plan** out) {
-  (void)flags;
-  return plan_1d_common(n, sign, howmany, precision, nullptr, 0, out);
+  return plan_1d_common(n, sign, howmany, precision, nullptr, 0, out, flags);
 }
 
 lfg_status lfg_plan_r2c(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
@@ -207,7 +250,6 @@ lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision
 // library executes.  Strides and offsets arrive in doubles.
 lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precision,
                          unsigned flags, lfg_plan** out) {
-  (void)flags;
   if (!out) return fail(LFG_ERR_INVALID, "null output handle");
   *out = nullptr;
   if (!spec || nspec < 8) return fail(LFG_ERR_INVALID, "spec too short");
@@ -308,6 +350,7 @@ lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precisi
   p.out.stride = os / 2;
   p.out.dist = vrank == 1 ? vos / 2 : 0;
   p.radices = lfg::choose_radices(n, precision);
+  p.measure = (flags & LFG_MEASURE) != 0;
   return finish_c2c(p, out);
 }
 
@@ -328,6 +371,15 @@ lfg_status lfg_execute_host(const lfg_plan* plan, const void* in, void* out) {
   const size_t sb = p.precision == 0 ? 8 : 4;
   const size_t ib = (size_t)p.in_span * sb, ob = (size_t)p.out_span * sb;
   cudaError_t e;
+  {
+    void* mi = mapped_device_ptr(in, ib);
+    void* mo = in == out ? mi : mapped_device_ptr(out, ob);
+    if (mi && mo) {   // pinned host buffers: the kernels stream them over NVLink-C2C
+      if ((e = lfg::execute_plan(p, mi, mo, 0, true)) != cudaSuccess) return cuda_fail(e, "execute");
+      if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return cuda_fail(e, "execute");
+      return LFG_OK;
+    }
+  }
   if (!p.d_host_in) {
     if ((e = cudaMalloc(&p.d_host_in, ib)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
     if ((e = cudaMalloc(&p.d_host_out, ob)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
@@ -445,6 +497,10 @@ lfg_status lfg_plan_ragged(const int64_t* sizes, size_t count, const int64_t* in
   if (!r.empty) {
     e = lfg::prepare_group_kernels_f64();
     if (e != cudaSuccess) return cuda_fail(e, "kernel set-up");
+    if (flags & LFG_MEASURE) {
+      std::string tm = lfg::tune_ragged(r, opt);
+      if (!tm.empty()) return fail(LFG_ERR_CUDA, tm);
+    }
     r.options = opt;
     std::string msg = lfg::build_ragged(r, opt);
     if (!msg.empty()) {
@@ -480,6 +536,15 @@ lfg_status lfg_execute_ragged_host(const lfg_ragged* plan, const void* in, void*
   const size_t es = r.precision == 0 ? 16 : 8;
   const size_t ib = (size_t)r.in_span * es, ob = (size_t)r.out_span * es;
   cudaError_t e;
+  {
+    void* mi = mapped_device_ptr(in, ib);
+    void* mo = mapped_device_ptr(out, ob);
+    if (mi && mo) {   // pinned host buffers: the kernel streams them over NVLink-C2C
+      if ((e = lfg::execute_ragged_mapped(r, mi, mo, 0)) != cudaSuccess) return cuda_fail(e, "execute ragged");
+      if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return cuda_fail(e, "execute ragged");
+      return LFG_OK;
+    }
+  }
   if (!r.d_host_in) {
     if ((e = cudaMalloc(&r.d_host_in, ib)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");
     if ((e = cudaMalloc(&r.d_host_out, ob)) != cudaSuccess) return cuda_fail(e, "cudaMalloc");

@@ -18,13 +18,20 @@ cudaError_t prepare_group_kernels_f64();
 cudaError_t launch_group_f64(const GroupDesc& g, bool fwd, const void* in, void* out,
                              cudaStream_t stream);
 
+// FP32 group kernel: 2 * C * M * 8 bytes of shared memory.
+cudaError_t prepare_group_kernels_f32();
+cudaError_t launch_group_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
+                             cudaStream_t stream);
+
 // Persistent FP64 kernel over a ragged batch (one launch for all sizes), in kRaggedVariants
 // block shapes (threads x minimum CTAs per SM).
 constexpr int kRaggedVariants = 5;
 size_t ragged_smem_bytes_f64(const RaggedClass& c);
 int ragged_variant_threads(int variant);
 int ragged_blocks_per_sm_f64(size_t smem, int variant);
+// scratch (optional): grid x slab complex elements of device memory; when given, two-group
+// items stage their intermediate there instead of in the output.
 cudaError_t launch_ragged_f64(const RaggedLaunch& r, bool fwd, const void* in, void* out,
-                              cudaStream_t stream);
+                              cudaStream_t stream, void* scratch = nullptr, int64_t slab = 0);
 
 }  // namespace lfg

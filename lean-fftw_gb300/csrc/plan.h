@@ -43,6 +43,10 @@ struct Plan {
   mutable void* d_host_in = nullptr;     // staging buffers of lfg_execute_host
   mutable void* d_host_out = nullptr;
   bool empty = false;    // a vector dimension of size 0: nothing to do
+  int64_t single_max = 0;  // largest size run as one pass group (0: as large as fits)
+  bool no_comp = false;    // binary32: no compensated twiddle passes
+  int64_t tile = 0;        // complex elements per CTA tile (0: the default)
+  bool measure = false;    // LFG_MEASURE: autotune before building
   // real transforms (kind R2C / C2R): rows of the last dimension, and for rank 2 the complex
   // transform along the first dimension (columns of the half spectrum)
   RealDesc real{};
@@ -99,6 +103,9 @@ void* upload_tables(const std::vector<double>& v, int precision, std::string* er
 
 void free_plan_memory(Plan& p);
 
-cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream);
+// force_scratch: keep the intermediate of two-group plans in the plan's device scratch even
+// out of place (used when `out` is host memory mapped into the device's address space).
+cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream,
+                         bool force_scratch = false);
 
 }  // namespace lfg

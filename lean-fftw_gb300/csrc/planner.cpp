@@ -161,12 +161,16 @@ void fill_group(GroupDesc& g, const std::vector<int>& rs, const PassTables& pt, 
   g.nsub = (int)nsub;
   int64_t cmax = std::max<int64_t>(1, tile_target / M);
   while (cmax > 1 && smem_bytes(cmax, M, precision) > kSmemBudget) --cmax;
-  g.C = (int)divisor_at_most(nsub, cmax);
+  // tiles may straddle lines (the sub-problem index is taken per element), so C need not
+  // divide nsub; prefer a divisor when one is close to the target
+  const int64_t dv = divisor_at_most(nsub, cmax);
+  g.C = (int)(2 * dv >= cmax ? dv : cmax);
   int64_t P0 = 1;
   for (int t = 0; t < t0; ++t) P0 *= rs[t];
   g.kmul = (int)P0;
   g.twsub = t0 > 0 ? 1 : 0;
   g.scale = 1.0;
+  for (int t = 0; t < kMaxPass; ++t) g.pass[t].comp = 0;
   for (int t = t0; t < t1; ++t) {
     PassDesc& d = g.pass[t - t0];
     d.R = rs[t];
@@ -224,6 +228,39 @@ int64_t max_single_group(int precision) {
   return (int64_t)(kSmemBudget / (2 * (precision == 0 ? 16 : 8)));
 }
 
+// binary32 plans of size >= 2^16 multiply by compensated (hi, lo) twiddles in their last
+// passes (the second group's, or the last two of a single group)
+std::vector<int> compensated_passes(int64_t N, const std::vector<int>& rs, int split, int precision) {
+  std::vector<int> comp(rs.size(), 0);
+  if (precision != 1 || N < (1 << 16)) return comp;
+  const int first = split < (int)rs.size() ? split : std::max(1, (int)rs.size() - 2);
+  for (int t = std::max(first, 1); t < (int)rs.size(); ++t) comp[t] = 1;
+  return comp;
+}
+
+// Re-lay the tables of compensated passes as [hi table | lo table] (binary32 parts of each
+// binary64 value: hi = fl32(v), lo = fl32(v - hi)); other tables stay binary64 and are rounded
+// on upload.  Returns the new table array, in binary64 scalars holding binary32-exact values.
+std::vector<double> split_compensated(PassTables& pt, const std::vector<int>& rs,
+                                      const std::vector<int>& comp) {
+  std::vector<double> out;
+  std::vector<size_t> off(rs.size(), 0);
+  for (size_t t = 1; t < rs.size(); ++t) {
+    const size_t len = 2 * (size_t)(rs[t] - 1) * pt.ns[t];
+    off[t] = out.size();
+    const double* v = pt.values.data() + pt.offset[t];
+    if (comp[t]) {
+      for (size_t i = 0; i < len; ++i) out.push_back((double)(float)v[i]);
+      for (size_t i = 0; i < len; ++i) out.push_back((double)(float)(v[i] - (double)(float)v[i]));
+    } else {
+      for (size_t i = 0; i < len; ++i) out.push_back(v[i]);
+    }
+    while (out.size() % 4) out.push_back(0.0);
+  }
+  pt.offset = off;
+  return out;
+}
+
 std::string build_c2c(Plan& p, int64_t tile_target) {
   const int64_t N = p.n;
   const int prec = p.precision;
@@ -232,9 +269,13 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   if (!msg.empty()) return msg;
   // pass grouping: one group when a transform fits one CTA's shared memory, else split the
   // sequence after the prefix whose product P best balances P against N/P
-  const int split = split_point(N, rs, max_single_group(prec));
+  const int64_t single = p.single_max > 0 ? std::min(p.single_max, max_single_group(prec))
+                                          : max_single_group(prec);
+  const int split = split_point(N, rs, single);
   if (split < 0) return "size too large for two pass groups with this radix order";
   PassTables pt = make_pass_tables(N, p.fwd, rs, prec);
+  const std::vector<int> comp = compensated_passes(N, rs, split, p.no_comp ? 0 : prec);
+  if (prec == 1) pt.values = split_compensated(pt, rs, comp);
   p.d_twiddles = upload_tables(pt.values, prec, &msg);
   if (!p.d_twiddles) return msg;
 
@@ -278,6 +319,9 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
     p.group_first_pass[0] = 0;
     p.group_first_pass[1] = split;
   }
+  for (int gi = 0; gi < p.ngroups; ++gi)
+    for (int t = 0; t < p.groups[gi].npass; ++t)
+      p.groups[gi].pass[t].comp = comp[p.group_first_pass[gi] + t];
   return "";
 }
 
@@ -382,7 +426,8 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
   return "";
 }
 
-cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream) {
+cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream,
+                         bool force_scratch) {
   if (p.empty) return cudaSuccess;
   if (p.kind == Kind::R2C) {
     cudaError_t e = launch_real_f64(p.real, true, in, out, stream);
@@ -403,7 +448,7 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
   char* ob = static_cast<char*>(out) + p.out.offset * (int64_t)es;
   auto launch = [&](const GroupDesc& g, const void* a, void* b) -> cudaError_t {
     if (p.precision == 0) return launch_group_f64(g, p.fwd, a, b, stream);
-    return cudaErrorNotSupported;
+    return launch_group_f32(g, p.fwd, a, b, stream);
   };
   if (p.ngroups == 1) return launch(p.groups[0], ib, ob);
   // two groups: the intermediate goes to `out` when it does not alias the input, else to the
@@ -412,7 +457,7 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
   const int64_t P = g2.nsub;
   char* zb;
   int64_t z_line, z_stride;
-  if (in != out) {
+  if (in != out && !force_scratch) {
     zb = ob;
     z_line = p.out.dist;
     z_stride = p.out.stride;

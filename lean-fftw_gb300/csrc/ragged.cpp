@@ -29,8 +29,9 @@ void free_ragged(RaggedPlan& r) {
   if (r.graph_exec) cudaGraphExecDestroy(r.graph_exec);
   if (r.capture_stream) cudaStreamDestroy(r.capture_stream);
   for (void* p : {r.d_twiddles, r.d_classes, r.d_items, r.d_in_off, r.d_out_off, r.d_counter,
-                  r.d_host_in, r.d_host_out})
+                  r.d_host_in, r.d_host_out, r.d_slabs})
     if (p) cudaFree(p);
+  r.d_slabs = nullptr;
   r.graph_exec = nullptr;
   r.capture_stream = nullptr;
   r.d_twiddles = r.d_classes = r.d_items = r.d_in_off = r.d_out_off = r.d_counter = nullptr;
@@ -258,6 +259,25 @@ cudaError_t execute_ragged_direct(const RaggedPlan& r, const void* in, void* out
   cudaError_t e = cudaMemsetAsync(r.d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   return launch_ragged_f64(r.launch, r.fwd, in, out, s);
+}
+
+cudaError_t execute_ragged_mapped(const RaggedPlan& r, const void* in, void* out, cudaStream_t s) {
+  // the largest two-group size sets the slab of each persistent CTA
+  int64_t slab = 0;
+  for (size_t c = 0; c < r.classes_host.size(); ++c)
+    if (r.classes_host[c].ngroups == 2) slab = std::max<int64_t>(slab, r.class_n[c]);
+  const size_t need = (size_t)slab * r.launch.grid * (r.precision == 0 ? 16 : 8);
+  if (need > r.slab_bytes) {
+    if (r.d_slabs) cudaFree(r.d_slabs);
+    r.d_slabs = nullptr;
+    r.slab_bytes = 0;
+    cudaError_t e = cudaMalloc(&r.d_slabs, need);
+    if (e != cudaSuccess) return e;
+    r.slab_bytes = need;
+  }
+  cudaError_t e = cudaMemsetAsync(r.d_counter, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  return launch_ragged_f64(r.launch, r.fwd, in, out, s, slab ? r.d_slabs : nullptr, slab);
 }
 
 cudaError_t execute_ragged(const RaggedPlan& r, const void* in, void* out, cudaStream_t s) {

@@ -48,6 +48,8 @@ struct RaggedPlan {
   void *d_twiddles = nullptr, *d_classes = nullptr, *d_items = nullptr, *d_in_off = nullptr,
        *d_out_off = nullptr, *d_counter = nullptr;
   mutable void *d_host_in = nullptr, *d_host_out = nullptr;
+  mutable void* d_slabs = nullptr;                     // per-CTA intermediates (host-mapped runs)
+  mutable size_t slab_bytes = 0;
   mutable cudaGraphExec_t graph_exec = nullptr;
   mutable cudaStream_t capture_stream = nullptr;
   mutable const void* graph_in = nullptr;
@@ -56,6 +58,9 @@ struct RaggedPlan {
 
 std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt);
 cudaError_t execute_ragged(const RaggedPlan& r, const void* in, void* out, cudaStream_t s);
+// Direct launch whose two-group items keep their intermediate in device slabs, so `in` and
+// `out` may be host memory mapped into the device's address space.
+cudaError_t execute_ragged_mapped(const RaggedPlan& r, const void* in, void* out, cudaStream_t s);
 void free_ragged(RaggedPlan& r);
 
 }  // namespace lfg

@@ -17,7 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "real.h"
-#include "stockham_f64.cuh"
+#include "stockham_dev.cuh"
 
 namespace lfg {
 using namespace dev;

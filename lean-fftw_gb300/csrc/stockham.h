@@ -34,8 +34,9 @@ struct PassDesc {
   int R;                 // radix of the pass
   int ns_loc;            // product of the group's earlier radices
   int ns_g;              // product of all earlier radices of the transform (table row length)
-  int pad_;
-  const void* tw;        // pass twiddle table (2*(R-1)*ns_g scalars), nullptr for pass 0
+  int comp;              // binary32 only: twiddles as (hi, lo) pairs, compensated products
+  const void* tw;        // pass twiddle table (2*(R-1)*ns_g scalars; binary32 comp passes:
+                         // the hi table followed by the lo table), nullptr for pass 0
 };
 
 // Complex element (s, i) of sub-problem s (flattened over lines) lives at

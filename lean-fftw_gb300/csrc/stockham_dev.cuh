@@ -1,0 +1,238 @@
+// Device-side building blocks of the Stockham kernels (pass, tile copy, tile driver), for
+// binary64 (T = double) and binary32 (T = float).
+//
+// Each butterfly is a generated codelet (generated/codelets_f{64,32}.cuh) evaluated with
+// explicitly rounded IEEE operations, so each binary64 pass performs exactly the operations
+// of lean-fftw's reference pass (`LeanFFTW/Gen/Stockham.lean:263-284`); stockham.h explains
+// why grouping passes over sub-problems preserves this.  The binary32 passes run the same
+// operation DAGs in binary32, with twiddles rounded from the binary64 tables; passes marked
+// `comp` multiply by twiddles held as two binary32 parts (hi + lo) with compensated products.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "generated/codelets_f32.cuh"
+#include "generated/codelets_f64.cuh"
+#include "kernels.h"
+#include "stockham.h"
+
+namespace lfg {
+namespace dev {
+
+template <class T>
+struct Prec;
+
+template <>
+struct Prec<double> {
+  using C = double2;
+  template <bool F, int R, bool W>
+  using Bfly = BflyD<F, R, W>;
+  static __device__ __forceinline__ C mk(double a, double b) { return make_double2(a, b); }
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+};
+
+template <>
+struct Prec<float> {
+  using C = float2;
+  template <bool F, int R, bool W>
+  using Bfly = BflyF<F, R, W>;
+  static __device__ __forceinline__ C mk(float a, float b) { return make_float2(a, b); }
+  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+};
+
+
+// One pass over the C sub-problems of a tile: src, dst are tile buffers in shared memory.
+// MODE 0: untwiddled; 1: twiddled codelet (table twiddles); 2: compensated twiddle products
+// with (hi, lo) binary32 twiddles, then the untwiddled codelet.
+template <class T, bool FWD, int R, int MODE>
+__device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ src,
+                                       typename Prec<T>::C* __restrict__ dst, int C, int M,
+                                       const PassDesc& pd, int kmul, int64_t msub0, int nsub) {
+  using P = Prec<T>;
+  using Cx = typename P::C;
+  constexpr bool TW = MODE == 1;
+  const int MR = M / R;
+  const int nb = C * MR;
+  const int ns = pd.ns_loc;
+  const T* __restrict__ tw = static_cast<const T*>(pd.tw);
+  const int64_t nsg = pd.ns_g;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+    const int c = q / MR;
+    const int j = q - c * MR;
+    T x[TW ? 4 * R - 2 : 2 * R];
+    T y[2 * R];
+    const Cx* s = src + c * M + j;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const Cx v = s[r * MR];
+      x[2 * r] = v.x;
+      x[2 * r + 1] = v.y;
+    }
+    const int k = j % ns;
+    // table index of the twiddle: k_loc * kmul + sub-problem index (second group only)
+    // (msub0 >= 0: first sub-problem of the tile, flattened over lines; tiles may straddle lines)
+    const int64_t kg = (int64_t)k * kmul + (msub0 >= 0 ? (msub0 + c) % nsub : 0);
+    if (MODE == 1) {
+#pragma unroll
+      for (int r = 0; r < R - 1; ++r) {
+        x[2 * R + 2 * r] = __ldg(tw + 2 * r * nsg + kg);
+        x[2 * R + 2 * r + 1] = __ldg(tw + (2 * r + 1) * nsg + kg);
+      }
+    } else if (MODE == 2) {
+      // w = (wr_hi + wr_lo) + i (wi_hi + wi_lo); the lo parts follow the hi table
+      const T* __restrict__ lo = tw + 2 * (int64_t)(R - 1) * nsg;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const T wrh = __ldg(tw + 2 * (r - 1) * nsg + kg), wih = __ldg(tw + (2 * r - 1) * nsg + kg);
+        const T wrl = __ldg(lo + 2 * (r - 1) * nsg + kg), wil = __ldg(lo + (2 * r - 1) * nsg + kg);
+        const T a = x[2 * r], b = x[2 * r + 1];
+        const T cr = P::fma(a, wrl, -P::mul(b, wil));          // small correction terms
+        const T ci = P::fma(a, wil, P::mul(b, wrl));
+        x[2 * r] = P::fma(a, wrh, P::fma(-b, wih, cr));
+        x[2 * r + 1] = P::fma(a, wih, P::fma(b, wrh, ci));
+      }
+    }
+    P::template Bfly<FWD, R, TW>::run(x, y);
+    const int b = j / ns;
+    Cx* d = dst + c * M + b * ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[r * ns] = P::mk(y[2 * r], y[2 * r + 1]);
+  }
+}
+
+template <class T, bool FWD>
+__device__ __forceinline__ void run_pass_t(const typename Prec<T>::C* src, typename Prec<T>::C* dst,
+                                           int C, int M, const PassDesc& pd, int kmul,
+                                           int64_t msub0, int nsub) {
+#define LFG_PASS_CASE(RR)                                                              \
+  case RR:                                                                             \
+    if (!pd.tw) pass_t<T, FWD, RR, 0>(src, dst, C, M, pd, kmul, msub0, nsub);          \
+    else if (sizeof(T) == 4 && pd.comp) pass_t<T, FWD, RR, 2>(src, dst, C, M, pd, kmul, msub0, nsub); \
+    else pass_t<T, FWD, RR, 1>(src, dst, C, M, pd, kmul, msub0, nsub);                 \
+    break;
+  switch (pd.R) {
+    LFG_PASS_CASE(2)
+    LFG_PASS_CASE(3)
+    LFG_PASS_CASE(4)
+    LFG_PASS_CASE(5)
+    LFG_PASS_CASE(6)
+    LFG_PASS_CASE(7)
+    LFG_PASS_CASE(8)
+    LFG_PASS_CASE(9)
+    LFG_PASS_CASE(10)
+    LFG_PASS_CASE(11)
+    LFG_PASS_CASE(12)
+    LFG_PASS_CASE(13)
+    LFG_PASS_CASE(14)
+    LFG_PASS_CASE(15)
+    LFG_PASS_CASE(16)
+    default: break;   // rejected by the planner
+  }
+#undef LFG_PASS_CASE
+}
+
+// Line bases (complex-element offsets of each line) of the two tile sources: evenly strided
+// lines of a batched plan, or a list of per-transform offsets of a ragged batch.
+struct StridedLines {
+  int64_t in_line, out_line;
+  __device__ int64_t in(int64_t line) const { return line * in_line; }
+  __device__ int64_t out(int64_t line) const { return line * out_line; }
+};
+
+struct ListedLines {
+  const int64_t* __restrict__ in_off;
+  const int64_t* __restrict__ out_off;
+  int64_t first;
+  __device__ int64_t in(int64_t line) const { return __ldg(in_off + first + line); }
+  __device__ int64_t out(int64_t line) const { return __ldg(out_off + first + line); }
+};
+
+// Copy a tile between global memory and a shared-memory tile buffer; the loop order makes
+// consecutive threads touch consecutive global addresses (elements of a sub-problem when
+// they are contiguous, else neighbouring sub-problems).
+template <class T, bool LOAD, class Lines>
+__device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typename Prec<T>::C* gin,
+                                          typename Prec<T>::C* gout, const GroupDesc& g,
+                                          const Lines& lines, int64_t s0, int C) {
+  using P = Prec<T>;
+  const int64_t sub_st = LOAD ? g.in_sub : g.out_sub;
+  const int64_t elem_st = LOAD ? g.in_elem : g.out_elem;
+  const int M = g.M;
+  const int nsub = g.nsub;
+  const int n = C * M;
+  const bool elem_fast = (elem_st == 1);
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    int c, i;
+    if (elem_fast) {
+      c = idx / M;
+      i = idx - c * M;
+    } else {
+      i = idx / C;
+      c = idx - i * C;
+    }
+    const int64_t s = s0 + c;
+    const int64_t line = s / nsub;
+    const int64_t sub = s - line * nsub;
+    const int64_t a = (LOAD ? lines.in(line) : lines.out(line)) + sub * sub_st + (int64_t)i * elem_st;
+    if (LOAD) {
+      tile[c * M + i] = gin[a];
+    } else if (g.scale == 1.0) {
+      gout[a] = tile[c * M + i];
+    } else {
+      const auto v = tile[c * M + i];
+      const T sc = (T)g.scale;
+      gout[a] = P::mk(P::mul(v.x, sc), P::mul(v.y, sc));
+    }
+  }
+}
+
+// Run every pass of group g on a tile of C sub-problems held in shared-memory buffer A
+// (B is the ping-pong partner); returns the buffer holding the result.
+template <class T, bool FWD>
+__device__ __forceinline__ typename Prec<T>::C* run_passes(const GroupDesc& g,
+                                                           typename Prec<T>::C* A,
+                                                           typename Prec<T>::C* B, int C,
+                                                           int64_t msub0) {
+  const int npass = g.npass;
+  for (int t = 0; t < npass; ++t) {
+    run_pass_t<T, FWD>(A, B, C, g.M, g.pass[t], g.kmul, msub0, g.nsub);
+    __syncthreads();
+    auto tmp = A;
+    A = B;
+    B = tmp;
+  }
+  return A;
+}
+
+// Load C sub-problems starting at s0, run every pass of group g in shared memory, store.
+template <class T, bool FWD, class Lines>
+__device__ __forceinline__ void process_tile(const GroupDesc& g, const Lines& lines, int64_t s0,
+                                             int C, const typename Prec<T>::C* in,
+                                             typename Prec<T>::C* out, typename Prec<T>::C* smem) {
+  auto* A = smem;
+  auto* B = smem + (size_t)g.C * g.M;
+  copy_tile<T, true>(A, in, nullptr, g, lines, s0, C);
+  __syncthreads();
+  // second group: the sub-problem index within the line enters the twiddle index
+  const int64_t msub0 = g.twsub ? s0 : -1;
+  A = run_passes<T, FWD>(g, A, B, C, msub0);
+  copy_tile<T, false>(A, nullptr, out, g, lines, s0, C);
+}
+
+// binary64 names used by the FP64 kernels
+template <bool FWD>
+__device__ __forceinline__ double2* run_passes_f64(const GroupDesc& g, double2* A, double2* B,
+                                                   int C, int64_t msub0) {
+  return run_passes<double, FWD>(g, A, B, C, msub0);
+}
+
+template <bool FWD, class Lines>
+__device__ __forceinline__ void process_tile_f64(const GroupDesc& g, const Lines& lines,
+                                                 int64_t s0, int C, const double2* in,
+                                                 double2* out, double2* smem) {
+  process_tile<double, FWD>(g, lines, s0, C, in, out, smem);
+}
+
+}  // namespace dev
+}  // namespace lfg

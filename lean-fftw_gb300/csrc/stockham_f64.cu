@@ -15,7 +15,7 @@
 
 #include <algorithm>
 
-#include "stockham_f64.cuh"
+#include "stockham_dev.cuh"
 
 namespace lfg {
 using namespace dev;
@@ -37,12 +37,20 @@ group_kernel_f64(const GroupDesc g, const double2* in, double2* out) {
 // first group writes its intermediate to the output and whose second group then works on
 // the output in place; the barrier between them orders the global-memory traffic within
 // the CTA.  Items are sorted by decreasing cost, so the largest start first.
+// One fixed base per side (a single line): the two-group items that stage their
+// intermediate in a CTA-private scratch slab instead of the output.
+struct FixedBases {
+  int64_t in_base, out_base;
+  __device__ int64_t in(int64_t) const { return in_base; }
+  __device__ int64_t out(int64_t) const { return out_base; }
+};
+
 template <bool FWD, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __restrict__ items,
                   int nitems, const int64_t* __restrict__ in_off,
                   const int64_t* __restrict__ out_off, const double2* in, double2* out,
-                  unsigned int* counter) {
+                  unsigned int* counter, double2* scratch, int64_t slab) {
   extern __shared__ double2 smem_f64[];
   __shared__ int s_item;
   for (;;) {
@@ -55,17 +63,32 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
     const ListedLines lines{in_off, out_off, w.first};
     if (rc.ngroups == 1) {
       process_tile_f64<FWD>(rc.g[0], lines, 0, w.count, in, out, smem_f64);
+    } else if (scratch) {
+      // intermediate in this CTA's slab of device memory (the output may be host memory)
+      const GroupDesc& g1 = rc.g[0];
+      const GroupDesc& g2 = rc.g[1];
+      double2* mine = scratch + (int64_t)blockIdx.x * slab;
+      const FixedBases first{__ldg(in_off + w.first), 0};
+      const FixedBases second{0, __ldg(out_off + w.first)};
+      for (int64_t s0 = 0; s0 < g1.nsub; s0 += g1.C) {
+        process_tile_f64<FWD>(g1, first, s0, (int)min((int64_t)g1.C, g1.nsub - s0), in, mine, smem_f64);
+        __syncthreads();
+      }
+      for (int64_t s0 = 0; s0 < g2.nsub; s0 += g2.C) {
+        process_tile_f64<FWD>(g2, second, s0, (int)min((int64_t)g2.C, g2.nsub - s0), mine, out, smem_f64);
+        __syncthreads();
+      }
     } else {
       const GroupDesc& g1 = rc.g[0];
       const GroupDesc& g2 = rc.g[1];
       for (int64_t s0 = 0; s0 < g1.nsub; s0 += g1.C) {
-        process_tile_f64<FWD>(g1, lines, s0, g1.C, in, out, smem_f64);
+        process_tile_f64<FWD>(g1, lines, s0, (int)min((int64_t)g1.C, g1.nsub - s0), in, out, smem_f64);
         __syncthreads();
       }
       // the second group reads the first group's result from the output
       const ListedLines inner{out_off, out_off, w.first};
       for (int64_t s0 = 0; s0 < g2.nsub; s0 += g2.C) {
-        process_tile_f64<FWD>(g2, inner, s0, g2.C, out, out, smem_f64);
+        process_tile_f64<FWD>(g2, inner, s0, (int)min((int64_t)g2.C, g2.nsub - s0), out, out, smem_f64);
         __syncthreads();
       }
     }
@@ -86,7 +109,8 @@ size_t ragged_smem_bytes_f64(const RaggedClass& c) {
 // Block shapes of the persistent kernel the autotuner chooses from: (threads, minimum
 // resident CTAs per SM, which caps the registers per thread).
 using RaggedFn = void (*)(const RaggedClass*, const RaggedItem*, int, const int64_t*,
-                          const int64_t*, const double2*, double2*, unsigned int*);
+                          const int64_t*, const double2*, double2*, unsigned int*, double2*,
+                          int64_t);
 
 template <bool FWD>
 RaggedFn ragged_fn(int variant) {
@@ -110,12 +134,12 @@ int ragged_variant_threads(int variant) {
 }
 
 cudaError_t launch_ragged_f64(const RaggedLaunch& r, bool fwd, const void* in, void* out,
-                              cudaStream_t stream) {
+                              cudaStream_t stream, void* scratch, int64_t slab) {
   if (r.nitems <= 0) return cudaSuccess;
   RaggedFn kern = fwd ? ragged_fn<true>(r.variant) : ragged_fn<false>(r.variant);
   kern<<<r.grid, ragged_variant_threads(r.variant), r.smem, stream>>>(
       r.classes, r.items, r.nitems, r.in_off, r.out_off, static_cast<const double2*>(in),
-      static_cast<double2*>(out), r.counter);
+      static_cast<double2*>(out), r.counter, static_cast<double2*>(scratch), slab);
   return cudaGetLastError();
 }
 

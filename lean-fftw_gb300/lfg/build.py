@@ -55,6 +55,7 @@ def generate() -> None:
 
     os.makedirs(GEN, exist_ok=True)
     _write_if_changed(os.path.join(GEN, "codelets_f64.cuh"), cuda_codelets(GPU_RADICES, fp32=False))
+    _write_if_changed(os.path.join(GEN, "codelets_f32.cuh"), cuda_codelets(GPU_RADICES, fp32=True))
     un = [0] * 17
     tw = [0] * 17
     for R in GPU_RADICES:
@@ -86,7 +87,7 @@ def _digest(paths) -> str:
 def compile_all(verbose: bool = False, jobs: int = 8) -> str:
     os.makedirs(BUILD, exist_ok=True)
     cu, cpp = _sources()
-    headers = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".h", ".cuh"))]
     headers += [os.path.join(GEN, f) for f in sorted(os.listdir(GEN))]
     headers.append(os.path.join(REPO, "include", "lfg.h"))
     common = _digest(headers + [os.path.abspath(__file__)])

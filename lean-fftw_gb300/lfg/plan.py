@@ -93,16 +93,19 @@ def _prec(precision) -> int:
 
 
 def plan_1d(n: int, sign: int = -1, howmany: int = 1, precision="f64",
-            radices: Optional[Sequence[int]] = None, measure: bool = False) -> Plan:
-    """1-D complex transform of size n on `howmany` contiguous lines."""
+            radices: Optional[Sequence[int]] = None, measure: bool = False,
+            compensated: bool = True) -> Plan:
+    """1-D complex transform of size n on `howmany` contiguous lines.  Binary32 plans of
+    size >= 2^16 use compensated twiddle products in their last passes unless
+    compensated=False."""
     h = ctypes.c_void_p()
     if radices is not None:
         arr = (ctypes.c_int * len(radices))(*[int(r) for r in radices])
         check(lib().lfg_plan_1d_radices(n, sign, howmany, _prec(precision), arr, len(radices),
                                         ctypes.byref(h)))
     else:
-        check(lib().lfg_plan_1d(n, sign, howmany, _prec(precision),
-                                LFG_MEASURE if measure else LFG_ESTIMATE, ctypes.byref(h)))
+        flags = (LFG_MEASURE if measure else LFG_ESTIMATE) | (0 if compensated else 16)
+        check(lib().lfg_plan_1d(n, sign, howmany, _prec(precision), flags, ctypes.byref(h)))
     return Plan(h)
 
 

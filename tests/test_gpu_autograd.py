@@ -89,9 +89,10 @@ def test_r2c_c2r_gradients():
     err = np.linalg.norm(g.cpu().numpy() - ref) / np.linalg.norm(ref)
     assert err <= 1e-13, err
 
-    # c2r: loss = sum (w * irfft(h))^2
+    # c2r: loss = sum (w * irfft(h))^2, with h scaled so that irfft(h) = O(1): the loss must
+    # not dwarf its own h-perturbation, or binary64 cannot resolve the difference quotient
     w = torch.from_numpy(rng.standard_normal((B, n))).cuda()
-    h0 = np.fft.rfft(rng.random((B, n)) - 0.5)
+    h0 = np.fft.rfft(rng.random((B, n)) - 0.5) / n
     h = torch.from_numpy(h0).cuda().requires_grad_(True)
     loss2 = lambda z: torch.sum((w * T.irfft(z, n)) ** 2)
     loss2(h).backward()

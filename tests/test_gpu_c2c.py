@@ -155,3 +155,21 @@ def test_execute_host_roundtrip():
     assert _bits_equal(y, O.ref_transform(True, N, plan.radices, x))
     inv = lfg.plan_1d(N, 1, B).execute_host(y)
     assert np.max(np.abs(inv / N - x)) < 1e-14
+
+
+@pytest.mark.parametrize("N", [64, 1000, 4096, 10368])
+def test_measured_plans_bitexact(N, tmp_path, monkeypatch):
+    """LFG_MEASURE times candidate (radices, grouping, tile) plans; whatever it keeps must
+    still be the reference transform of its radix sequence, bit for bit, and every measured
+    candidate is logged (LF_PLAN_LOG analogue)."""
+    log = tmp_path / "plan.log"
+    monkeypatch.setenv("LFG_PLAN_LOG", str(log))
+    B = max(1, (1 << 16) // N)
+    plan = lfg.plan_1d(N, -1, B, measure=True)
+    x = O.uniform_complex((B, N), seed=N + 3)
+    y, ok = _run(plan, x)
+    assert ok
+    assert _bits_equal(y, O.ref_transform(True, N, plan.radices, x, nthreads=8))
+    lines = [json.loads(l) for l in open(log)]
+    assert lines and all(d["n"] == N for d in lines)
+    assert min(d["ms"] for d in lines) > 0

@@ -1,0 +1,48 @@
+"""The binary32 variant: error against the extended-precision oracle, per size.
+
+Twiddles come from the binary64 exact-integer tables (rounded to binary32); sizes >= 2^16
+use compensated (hi, lo) twiddle products in their last passes.  The error is measured
+against the double-double DFT of the same (binary32) input and must stay at the binary32
+level (a few times 2^-24); compensation must not be worse than plain products.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no GPU", allow_module_level=True)
+
+import lfg  # noqa: E402
+import oracle as O  # noqa: E402
+
+U32 = 2.0 ** -24
+
+
+def _run(n, B, x, sign=-1, compensated=True):
+    plan = lfg.plan_1d(n, sign, B, precision="f32", compensated=compensated)
+    xd = torch.from_numpy(x.astype(np.complex64)).cuda()
+    y = plan.execute(xd)
+    torch.cuda.synchronize()
+    return y.cpu().numpy().astype(np.complex128)
+
+
+@pytest.mark.parametrize("n", [2 ** k for k in range(1, 19)] + [6, 60, 360, 1000, 10368, 75600])
+def test_fp32_error_per_size(n):
+    B = max(1, min(8, (1 << 17) // n))
+    x = O.uniform_complex((B, n), seed=n).astype(np.complex64).astype(np.complex128)
+    for sign in (-1, 1):
+        y = _run(n, B, x, sign)
+        e = O.rel_l2(y, O.dd_dft(sign < 0, x, nthreads=8))
+        assert e < 4 * U32 * max(1.0, np.sqrt(np.log2(n))), (n, sign, e)
+
+
+@pytest.mark.parametrize("n", [1 << 16, 1 << 17, 1 << 18])
+def test_compensation_helps_large_sizes(n):
+    B = 2
+    x = O.uniform_complex((B, n), seed=7).astype(np.complex64).astype(np.complex128)
+    ref = O.dd_dft(True, x, nthreads=8)
+    e_comp = O.rel_l2(_run(n, B, x, compensated=True), ref)
+    e_plain = O.rel_l2(_run(n, B, x, compensated=False), ref)
+    assert e_comp <= e_plain * 1.02, (e_comp, e_plain)

@@ -93,3 +93,14 @@ def test_ragged_host_entry():
     for o, n in zip(off, sizes):
         ref = O.ref_transform(False, int(n), plan.radices(int(n)), x[o: o + n])
         assert np.array_equal(y[o: o + n].view(np.uint64), ref.view(np.uint64))
+
+
+def test_ragged_measured_plan_bitexact():
+    sizes = lfg.ragged_sizes(512, seed=11)
+    plan = lfg.plan_ragged(sizes, -1, measure=True)
+    x = O.uniform_complex((int(sizes.sum()),), seed=12)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    plan.execute(xd, yd)
+    torch.cuda.synchronize()
+    assert not _check(plan, sizes, x, yd.cpu().numpy(), plan.in_offsets, plan.out_offsets)
