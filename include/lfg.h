@@ -96,6 +96,20 @@ lfg_status lfg_set_scale(lfg_plan *plan, double scale);
  * for device-resident data. */
 lfg_status lfg_execute(const lfg_plan *plan, const void *in, void *out, void *stream);
 
+/* In-place execution of a complex plan that allocates nothing.  No counterpart in the
+ * reference: lean-fftw has no device memory to manage.  lfg_execute allocates a plan's
+ * scratch buffer with cudaMalloc the first time an in-place two-group plan (n above one
+ * CTA's shared memory) runs; callers that cannot allocate device memory themselves (runtimes
+ * that route all device memory through their own pool and forbid cudaMalloc, or steady-state
+ * loops that cannot take its implicit device synchronisation) use this entry point instead.
+ * The intermediate goes to a 16 MiB array in static device memory (held by every GPU that
+ * loads the library until the process exits), so n * howmany * (16 or 8) bytes must not exceed
+ * 16 MiB for two-group plans (LFG_ERR_UNSUPPORTED otherwise).  The array's device address is
+ * looked up on the first call on each device, so make that first call before any stream
+ * capture.  All calls share the one array: calls whose executions overlap on the GPU race on
+ * it.  `data` is the device buffer given to the plan as both input and output. */
+lfg_status lfg_execute_inplace_static(const lfg_plan *plan, void *data, void *stream);
+
 /* Execute on host pointers: copies the spanned input to the device, transforms, copies the
  * output back, and returns when the output is in `out`.  The host-memory analogue of
  * `lfa_call` (LeanFFTW/Asm/Kernels.lean:1203-1204) as called by the libbench2 backend

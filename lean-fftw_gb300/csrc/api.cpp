@@ -16,13 +16,7 @@
 #include "trig.h"
 #include "tuner.h"
 
-struct lfg_plan {
-  lfg::Plan p;
-};
-
-struct lfg_ragged {
-  lfg::RaggedPlan r;
-};
+#include "handles.h"
 
 namespace {
 
@@ -212,6 +206,8 @@ lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision prec
 }
 
 }  // namespace
+
+void lfg::set_last_error(const std::string& msg) { g_last_error = msg; }
 
 extern "C" {
 
