@@ -11,6 +11,13 @@ Workloads (synthetic inputs, re/im iid uniform[-0.5, 0.5) from numpy default_rng
              with one launch per distinct size is timed beside it (`per_size`).
   c2c_<N>    1-D complex FP64 forward, N = 2^k (k = 1..18), batch 2^26 / N (1 GiB in and
              out): the power-of-two sweep.
+  small_1024 one transform of N = 1024 (the plain small case: latency-bound).
+  large_262144[_f32]  32 transforms of N = 2^18, binary64 (or binary32: the FP32 variant with
+             compensated last-pass twiddles).
+  c2c_1024_f32  the binary32 variant at N = 1024, batch 2^17 (1 GiB in and out).
+  grad_4096  differentiation: batch 256 x N = 4096, loss = sum |W * FFT(x)|^2 (W iid complex
+             normal), one forward transform and one adjoint transform (the backward pass) per
+             step through torch.autograd; GFLOP/s counts both transforms.
 
 A step is one execution over the whole batch.  `value` is GFLOP/s with the conventional
 5 N log2 N flops per transform, inputs resident in HBM; `e2e` is the same metric through
@@ -45,6 +52,15 @@ SEED = 20261016
 WORKLOADS = {"ragged": dict(kind="ragged", count=8192, sign=-1)}
 for _k in range(1, 19):
     WORKLOADS[f"c2c_{1 << _k}"] = dict(kind="c2c", n=1 << _k, batch=(1 << 26) >> _k, sign=-1)
+# the other configurations of the reference's measurement plan, each as its own line
+WORKLOADS.update({
+    "small_1024": dict(kind="c2c", n=1024, batch=1, sign=-1),           # latency-bound
+    "large_262144": dict(kind="c2c", n=1 << 18, batch=32, sign=-1),
+    "large_262144_f32": dict(kind="c2c", n=1 << 18, batch=32, sign=-1, precision="f32"),
+    "c2c_1024_f32": dict(kind="c2c", n=1024, batch=1 << 17, sign=-1, precision="f32"),
+    # differentiation: loss = sum |W * FFT(x)|^2, forward transform + adjoint per step
+    "grad_4096": dict(kind="grad", n=4096, batch=256, sign=-1),
+})
 
 
 def peaks():
@@ -142,6 +158,23 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def max_over_ranks(value, device=None):
+    """Max of a per-rank scalar over the process group (identity when not distributed)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([float(value)], device=device or "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_seed(rank):
+    """Weak scaling: every rank transforms its own full per-GPU batch, seeded by rank; the
+    transforms are independent, so no data moves between ranks."""
+    return SEED + rank
 
 
 def cpu_reference(wl, steps, warmup, budget_s=None):
@@ -275,15 +308,8 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    def max_over_ranks(v):
-        if dist is None:
-            return v
-        t = torch.tensor([v], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
     stream = torch.cuda.current_stream()
-    rng = np.random.default_rng(SEED + rank)
+    rng = np.random.default_rng(rank_seed(rank))
     extra = {}
     if wl["kind"] == "ragged":
         sizes = ragged_workload_sizes(wl)
@@ -301,11 +327,40 @@ def main():
         extra["config_extra"] = {"distinct_sizes": int(rinfo.classes), "points": total,
                                  "work_items": int(rinfo.items), "grid": int(rinfo.grid),
                                  "smem_bytes": int(rinfo.smem_bytes)}
+    elif wl["kind"] == "grad":
+        from lfg import torch_ops
+        n, B = wl["n"], wl["batch"]
+        host = (rng.random((B, n, 2)) - 0.5).view(np.complex128).reshape(B, n)
+        W = torch.from_numpy((rng.standard_normal((B, n)) + 1j * rng.standard_normal((B, n)))).to(dev)
+        flops_step = 2 * flops_per_transform(n) * B      # forward + adjoint
+        points = 2 * n * B
+        launches_per_step = 2
+        fplan = lfg.plan_1d(n, -1, B)
+        codelet_ops = 2 * fplan.info().flops
+
+        def grad_step():
+            xg = x.detach().requires_grad_(True)
+            loss = torch.sum(torch.abs(W * torch_ops.fft(xg)) ** 2)
+            loss.backward()
+            return xg.grad
+
+        step_fn = grad_step
+
+        def host_fn(a, b):
+            xg = torch.from_numpy(a).to(dev, non_blocking=True).requires_grad_(True)
+            loss = torch.sum(torch.abs(W * torch_ops.fft(xg)) ** 2)
+            loss.backward()
+            b[...] = xg.grad.cpu().numpy()
+
+        extra["config_extra"] = {"loss": "sum |W * FFT(x)|^2", "radices": fplan.radices}
     else:
         n, B = wl["n"], wl["batch"]
-        plan = lfg.plan_1d(n, wl["sign"], B)
+        prec = wl.get("precision", "f64")
+        plan = lfg.plan_1d(n, wl["sign"], B, precision=prec)
         info = plan.info()
         host = (rng.random((B, n, 2)) - 0.5).view(np.complex128).reshape(B, n)
+        if prec == "f32":
+            host = host.astype(np.complex64)
         flops_step = flops_per_transform(n) * B
         points = n * B
         launches_per_step = int(info.ngroups)
@@ -321,7 +376,7 @@ def main():
 
     # headline: device-resident inputs
     ms, clocks = timed(step_fn, args.steps, stream, local, barrier)
-    ms = max_over_ranks(ms)
+    ms = max_over_ranks(ms, dev)
     value = flops_step * ws / (ms * 1e-3) / 1e9
 
     if wl["kind"] == "ragged":
@@ -330,7 +385,7 @@ def main():
         for _ in range(3):
             ps_step()
         ps_ms, _ = timed(ps_step, max(5, args.steps // 4), stream, local, barrier)
-        ps_ms = max_over_ranks(ps_ms)
+        ps_ms = max_over_ranks(ps_ms, dev)
         torch.cuda.synchronize()
         extra["per_size"] = {"value": round(flops_step * ws / (ps_ms * 1e-3) / 1e9, 3),
                              "unit": "GFLOP/s", "ms_per_step": round(ps_ms, 4),
@@ -340,7 +395,8 @@ def main():
                                                            y2.view(torch.float64)))}
 
     # roofline of the dominant kernel (one launch per step for ragged and single-group sizes)
-    alg_bytes = 32.0 * points            # read + write of the data once
+    esz = 8.0 if wl.get("precision") == "f32" else 16.0
+    alg_bytes = 2 * esz * points         # read + write of the data once
     hbm_peak, peak_kind = peaks()
     kernel_ms = ms / launches_per_step
     achieved = alg_bytes / launches_per_step / (kernel_ms * 1e-3) / 1e9
@@ -357,7 +413,7 @@ def main():
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         host_fn(hin_np, hout_np)
-    t_e2e = max_over_ranks((time.perf_counter() - t0) / e2e_steps)
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dev)
     e2e = flops_step * ws / t_e2e / 1e9
 
     cpu = None
@@ -371,22 +427,25 @@ def main():
         config.update(extra.pop("config_extra"))
         config["l2_flush"] = "inputs larger than L2 (129 MB)"
         config["parallelism"] = f"replicas{ws}"
+        metric = METRIC if wl.get("precision", "f64") == "f64" else METRIC.replace("FP64", "FP32")
         line = {
-            "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws,
+            "metric": metric, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": wl.get("precision", "f64"),
             "data": "synthetic", "config": config,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                          "peak_kind": peak_kind, "traffic": ncu_traffic(args.workload),
                          "algorithmic_bytes_per_launch": alg_bytes / launches_per_step},
-            "fp64_issue": {"achieved": round(fp64_ach, 4), "unit": "T FP64 instr/s",
+            "fp64_issue": None if wl.get("precision") == "f32" else
+                          {"achieved": round(fp64_ach, 4), "unit": "T FP64 instr/s",
                            "peak": fp64p, "frac": round(fp64_ach / fp64p, 4) if fp64p else None,
                            "note": "codelet binary64 instructions per step / step time; peak = "
                                    "measured DFMA issue rate (DADD/DMUL issue at 0.505)"},
             "e2e": {"value": round(e2e, 3), "unit": "GFLOP/s",
-                    "h2d_bytes_per_step": int(hin.numel() * 16),
-                    "d2h_bytes_per_step": int(hout.numel() * 16)},
+                    "h2d_bytes_per_step": int(hin.numel() * hin.element_size()),
+                    "d2h_bytes_per_step": int(hout.numel() * hout.element_size())},
             "gpu_launches": int(launches_per_step * args.steps),
             "cpu_baseline": cpu,
             "clocks": clocks,

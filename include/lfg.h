@@ -116,6 +116,11 @@ lfg_status lfg_execute_inplace_static(const lfg_plan *plan, void *data, void *st
  * (bench/backends/bench-leanfftw.c:284-288). */
 lfg_status lfg_execute_host(const lfg_plan *plan, const void *in, void *out);
 
+/* Synchronises with the device and reports whether a kernel of this plan gave up a bounded
+ * wait (LFG_ERR_TIMEOUT; the flag is then cleared).  The binary32 persistent kernel waits on
+ * its bulk copies with an iteration limit instead of spinning forever. */
+lfg_status lfg_device_status(const lfg_plan *plan);
+
 /* Release a plan and its device memory. */
 void lfg_destroy(lfg_plan *plan);
 

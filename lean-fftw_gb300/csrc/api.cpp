@@ -410,6 +410,20 @@ lfg_status lfg_set_scale(lfg_plan* plan, double scale) {
   return LFG_OK;
 }
 
+lfg_status lfg_device_status(const lfg_plan* plan) {
+  if (!plan) return fail(LFG_ERR_INVALID, "null plan");
+  const lfg::Plan& p = plan->p;
+  if (!p.d_status) return LFG_OK;
+  int v = 0;
+  cudaError_t e = cudaMemcpy(&v, p.d_status, sizeof v, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "status read");
+  if (v) {
+    cudaMemset(p.d_status, 0, sizeof v);
+    return fail(LFG_ERR_TIMEOUT, "a bounded device-side wait gave up (bulk copy not completed)");
+  }
+  return LFG_OK;
+}
+
 lfg_status lfg_get_plan_info(const lfg_plan* plan, lfg_plan_info* info) {
   if (!plan || !info) return fail(LFG_ERR_INVALID, "null argument");
   const lfg::Plan& p = plan->p;

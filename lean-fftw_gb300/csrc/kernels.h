@@ -23,6 +23,13 @@ cudaError_t prepare_group_kernels_f32();
 cudaError_t launch_group_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                              cudaStream_t stream);
 
+// Persistent FP32 kernel with bulk-async (TMA) prefetch for back-to-back lines of one group
+// (input and output 16-byte aligned, C*M even); *status = 1 if a bounded wait gave up.
+size_t stream_smem_bytes_f32(const GroupDesc& g);
+int stream_blocks_per_sm_f32(const GroupDesc& g);
+cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
+                              int64_t lines, unsigned grid, int* status, cudaStream_t stream);
+
 // Persistent FP64 kernel over a ragged batch (one launch for all sizes), in kRaggedVariants
 // block shapes (threads x minimum CTAs per SM).
 constexpr int kRaggedVariants = 5;

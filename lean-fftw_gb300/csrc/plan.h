@@ -47,6 +47,10 @@ struct Plan {
   bool no_comp = false;    // binary32: no compensated twiddle passes
   int64_t tile = 0;        // complex elements per CTA tile (0: the default)
   bool measure = false;    // LFG_MEASURE: autotune before building
+  // binary32 single-group plans over back-to-back lines run the persistent bulk-copy kernel
+  bool stream = false;
+  unsigned stream_grid = 0;
+  int* d_status = nullptr; // set to 1 on the device when a bounded wait gave up
   // real transforms (kind R2C / C2R): rows of the last dimension, and for rank 2 the complex
   // transform along the first dimension (columns of the half spectrum)
   RealDesc real{};

@@ -8,6 +8,7 @@
 // and LFG_MEASURE (api.cpp) times the leading candidates on the device.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <map>
 
@@ -70,7 +71,9 @@ int64_t divisor_at_most(int64_t n, int64_t cap) {
 }
 
 size_t smem_bytes(int64_t C, int64_t M, int precision) {
-  return 2 * (size_t)C * (size_t)M * (precision == 0 ? 16 : 8);
+  // two tile buffers, each padded by one element per 16 (stockham_dev.cuh: padded_elems)
+  const int64_t n = C * M;
+  return 2 * (size_t)(n + (n >> 4) + 1) * (precision == 0 ? 16 : 8);
 }
 
 std::vector<int> choose_radices(int64_t n, int precision) {
@@ -110,6 +113,8 @@ void free_plan_memory(Plan& p) {
   if (p.d_host_out) cudaFree(p.d_host_out);
   if (p.d_post) cudaFree(p.d_post);
   if (p.d_col_twiddles) cudaFree(p.d_col_twiddles);
+  if (p.d_status) cudaFree(p.d_status);
+  p.d_status = nullptr;
   p.d_twiddles = p.d_scratch = p.d_host_in = p.d_host_out = nullptr;
   p.d_post = p.d_col_twiddles = nullptr;
   if (cur != p.device) cudaSetDevice(cur);
@@ -225,7 +230,11 @@ void* upload_tables(const std::vector<double>& v, int precision, std::string* er
 }
 
 int64_t max_single_group(int precision) {
-  return (int64_t)(kSmemBudget / (2 * (precision == 0 ? 16 : 8)));
+  // largest n with two padded tile buffers within the budget
+  const int64_t es = precision == 0 ? 16 : 8;
+  int64_t n = (int64_t)(kSmemBudget / (2 * es));
+  while (n > 1 && smem_bytes(1, n, precision) > kSmemBudget) --n;
+  return n;
 }
 
 // binary32 plans of size >= 2^16 multiply by compensated (hi, lo) twiddles in their last
@@ -322,6 +331,22 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   for (int gi = 0; gi < p.ngroups; ++gi)
     for (int t = 0; t < p.groups[gi].npass; ++t)
       p.groups[gi].pass[t].comp = comp[p.group_first_pass[gi] + t];
+  // binary32 over back-to-back lines: the persistent kernel with bulk-copy prefetch
+  const GroupDesc& g0 = p.groups[0];
+  if (prec == 1 && p.ngroups == 1 && p.in.stride == 1 && p.out.stride == 1 && p.in.dist == N &&
+      p.out.dist == N && (N % 2) == 0 && p.howmany > 0 &&
+      smem_bytes(g0.C, g0.M, prec) * 2 <= kSmemBudget) {
+    if (cudaMalloc(&p.d_status, sizeof(int)) == cudaSuccess &&
+        cudaMemset(p.d_status, 0, sizeof(int)) == cudaSuccess) {
+      int dev = 0, sms = 1;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      const int64_t tiles = (p.howmany + g0.C - 1) / g0.C;
+      const int64_t want = (int64_t)sms * stream_blocks_per_sm_f32(g0);
+      p.stream_grid = (unsigned)std::max<int64_t>(1, std::min(want, tiles));
+      p.stream = true;
+    }
+  }
   return "";
 }
 
@@ -450,7 +475,14 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     if (p.precision == 0) return launch_group_f64(g, p.fwd, a, b, stream);
     return launch_group_f32(g, p.fwd, a, b, stream);
   };
-  if (p.ngroups == 1) return launch(p.groups[0], ib, ob);
+  if (p.ngroups == 1) {
+    // the bulk-copy engine needs 16-byte aligned ranges; in place is fine (each tile is read
+    // into shared memory before it is written)
+    if (p.stream && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)
+      return launch_stream_f32(p.groups[0], p.fwd, ib, ob, p.howmany, p.stream_grid, p.d_status,
+                               stream);
+    return launch(p.groups[0], ib, ob);
+  }
   // two groups: the intermediate goes to `out` when it does not alias the input, else to the
   // plan's scratch buffer (allocated on first use)
   GroupDesc g1 = p.groups[0], g2 = p.groups[1];

@@ -41,10 +41,10 @@ r2c_kernel_f64(const RealDesc d, const double* in, double2* out) {
   const int64_t l0 = (int64_t)blockIdx.x * g.C;
   const int C = (int)min((int64_t)g.C, d.lines - l0);
   double2* A = smem_f64;
-  double2* B = smem_f64 + (size_t)g.C * M;
+  double2* B = smem_f64 + padded_elems(g.C * M);
   for (int idx = threadIdx.x; idx < C * M; idx += blockDim.x) {
     const int c = idx / M, m = idx - c * M;
-    A[idx] = reinterpret_cast<const double2*>(in + real_base(d, l0 + c))[m];
+    A[spad(idx)] = reinterpret_cast<const double2*>(in + real_base(d, l0 + c))[m];
   }
   __syncthreads();
   const double2* F = run_passes_f64<true>(g, A, B, C, -1);
@@ -55,15 +55,15 @@ r2c_kernel_f64(const RealDesc d, const double* in, double2* out) {
   const int half = M / 2;
   for (int idx = threadIdx.x; idx < C * (half + 1); idx += blockDim.x) {
     const int c = idx / (half + 1), k = idx - c * (half + 1);
-    const double2* f = F + c * M;
+    const int f0 = c * M;
     double2* o = out + cplx_base(d, l0 + c);
     if (k == 0) {
-      const double2 z = f[0];
+      const double2 z = F[spad(f0)];
       o[0] = make_double2(__dadd_rn(z.x, z.y), 0.0);
       o[M] = make_double2(__dsub_rn(z.x, z.y), 0.0);
       continue;
     }
-    const double2 a = f[k], bc = f[M - k];
+    const double2 a = F[spad(f0 + k)], bc = F[spad(f0 + M - k)];
     const double sr = __dadd_rn(a.x, bc.x), si = __dsub_rn(a.y, bc.y);
     const double dr = __dsub_rn(a.x, bc.x), di = __dadd_rn(a.y, bc.y);
     const double2 w = __ldg(tw + k);
@@ -82,16 +82,16 @@ c2r_kernel_f64(const RealDesc d, const double2* in, double* out) {
   const int64_t l0 = (int64_t)blockIdx.x * g.C;
   const int C = (int)min((int64_t)g.C, d.lines - l0);
   double2* A = smem_f64;
-  double2* B = smem_f64 + (size_t)g.C * M;
+  double2* B = smem_f64 + padded_elems(g.C * M);
   const double2* __restrict__ tw = static_cast<const double2*>(d.post);   // (c, s)
   const int half = M / 2;
   for (int idx = threadIdx.x; idx < C * (half + 1); idx += blockDim.x) {
     const int c = idx / (half + 1), k = idx - c * (half + 1);
     const double2* h = in + cplx_base(d, l0 + c);
-    double2* z = A + c * M;
+    const int z0 = c * M;
     if (k == 0) {
       const double h0 = h[0].x, hm = h[M].x;   // imaginary parts ignored
-      z[0] = make_double2(__dadd_rn(h0, hm), __dsub_rn(h0, hm));
+      A[spad(z0)] = make_double2(__dadd_rn(h0, hm), __dsub_rn(h0, hm));
       continue;
     }
     double2 a = h[k], bc = h[M - k];
@@ -104,14 +104,14 @@ c2r_kernel_f64(const RealDesc d, const double2* in, double* out) {
     const double2 w = __ldg(tw + k);
     const double U = __fma_rn(w.x, di, __dmul_rn(w.y, dr));    // c di + s dr
     const double V = __fma_rn(w.x, dr, -__dmul_rn(w.y, di));   // c dr - s di
-    z[k] = make_double2(__dsub_rn(sr, U), __dadd_rn(si, V));
-    if (k != M - k) z[M - k] = make_double2(__dadd_rn(sr, U), __dsub_rn(V, si));
+    A[spad(z0 + k)] = make_double2(__dsub_rn(sr, U), __dadd_rn(si, V));
+    if (k != M - k) A[spad(z0 + M - k)] = make_double2(__dadd_rn(sr, U), __dsub_rn(V, si));
   }
   __syncthreads();
   const double2* F = run_passes_f64<false>(g, A, B, C, -1);
   for (int idx = threadIdx.x; idx < C * M; idx += blockDim.x) {
     const int c = idx / M, m = idx - c * M;
-    reinterpret_cast<double2*>(out + real_base(d, l0 + c))[m] = F[idx];
+    reinterpret_cast<double2*>(out + real_base(d, l0 + c))[m] = F[spad(idx)];
   }
 }
 
@@ -136,7 +136,7 @@ cudaError_t launch_real_f64(const RealDesc& d, bool r2c, const void* in, void* o
                             cudaStream_t stream) {
   const int64_t grid = (d.lines + d.g.C - 1) / d.g.C;
   if (grid <= 0) return cudaSuccess;
-  const size_t smem = 2 * (size_t)d.g.C * d.M * sizeof(double2);
+  const size_t smem = 2 * (size_t)padded_elems(d.g.C * d.M) * sizeof(double2);
   if (r2c)
     r2c_kernel_f64<<<(unsigned)grid, kGroupThreads, smem, stream>>>(
         d, static_cast<const double*>(in), static_cast<double2*>(out));

@@ -42,10 +42,17 @@ struct Prec<float> {
 };
 
 
-// One pass over the C sub-problems of a tile: src, dst are tile buffers in shared memory.
+// Shared-memory tiles are padded by one element after every 16: a Stockham pass stores its
+// outputs at stride R (up to 16 elements = 128 or 256 bytes) between neighbouring threads,
+// which would put a whole warp on one bank; with the padding the stride is 17 elements.
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int padded_elems(int n) { return n + (n >> 4) + 1; }
+
+// One pass over the C sub-problems of a tile: src, dst are tile buffers in shared memory
+// (dst padded; src padded unless SRCPAD is false, as for a stage buffer a bulk copy filled).
 // MODE 0: untwiddled; 1: twiddled codelet (table twiddles); 2: compensated twiddle products
 // with (hi, lo) binary32 twiddles, then the untwiddled codelet.
-template <class T, bool FWD, int R, int MODE>
+template <class T, bool FWD, int R, int MODE, bool SRCPAD = true>
 __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ src,
                                        typename Prec<T>::C* __restrict__ dst, int C, int M,
                                        const PassDesc& pd, int kmul, int64_t msub0, int nsub) {
@@ -62,10 +69,11 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
     const int j = q - c * MR;
     T x[TW ? 4 * R - 2 : 2 * R];
     T y[2 * R];
-    const Cx* s = src + c * M + j;
+    const int s0i = c * M + j;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const Cx v = s[r * MR];
+      const int si = s0i + r * MR;
+      const Cx v = src[SRCPAD ? spad(si) : si];
       x[2 * r] = v.x;
       x[2 * r + 1] = v.y;
     }
@@ -95,21 +103,21 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
     }
     P::template Bfly<FWD, R, TW>::run(x, y);
     const int b = j / ns;
-    Cx* d = dst + c * M + b * ns * R + k;
+    const int d0 = c * M + b * ns * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) d[r * ns] = P::mk(y[2 * r], y[2 * r + 1]);
+    for (int r = 0; r < R; ++r) dst[spad(d0 + r * ns)] = P::mk(y[2 * r], y[2 * r + 1]);
   }
 }
 
-template <class T, bool FWD>
+template <class T, bool FWD, bool SRCPAD = true>
 __device__ __forceinline__ void run_pass_t(const typename Prec<T>::C* src, typename Prec<T>::C* dst,
                                            int C, int M, const PassDesc& pd, int kmul,
                                            int64_t msub0, int nsub) {
-#define LFG_PASS_CASE(RR)                                                              \
-  case RR:                                                                             \
-    if (!pd.tw) pass_t<T, FWD, RR, 0>(src, dst, C, M, pd, kmul, msub0, nsub);          \
-    else if (sizeof(T) == 4 && pd.comp) pass_t<T, FWD, RR, 2>(src, dst, C, M, pd, kmul, msub0, nsub); \
-    else pass_t<T, FWD, RR, 1>(src, dst, C, M, pd, kmul, msub0, nsub);                 \
+#define LFG_PASS_CASE(RR)                                                                        \
+  case RR:                                                                                       \
+    if (!pd.tw) pass_t<T, FWD, RR, 0, SRCPAD>(src, dst, C, M, pd, kmul, msub0, nsub);            \
+    else if (sizeof(T) == 4 && pd.comp) pass_t<T, FWD, RR, 2, SRCPAD>(src, dst, C, M, pd, kmul, msub0, nsub); \
+    else pass_t<T, FWD, RR, 1, SRCPAD>(src, dst, C, M, pd, kmul, msub0, nsub);                   \
     break;
   switch (pd.R) {
     LFG_PASS_CASE(2)
@@ -138,6 +146,8 @@ struct StridedLines {
   int64_t in_line, out_line;
   __device__ int64_t in(int64_t line) const { return line * in_line; }
   __device__ int64_t out(int64_t line) const { return line * out_line; }
+  // line pitch of a side (lets a whole tile of back-to-back lines copy as one range)
+  __device__ int64_t pitch(bool load) const { return load ? in_line : out_line; }
 };
 
 struct ListedLines {
@@ -146,6 +156,7 @@ struct ListedLines {
   int64_t first;
   __device__ int64_t in(int64_t line) const { return __ldg(in_off + first + line); }
   __device__ int64_t out(int64_t line) const { return __ldg(out_off + first + line); }
+  __device__ int64_t pitch(bool) const { return -1; }
 };
 
 // Copy a tile between global memory and a shared-memory tile buffer; the loop order makes
@@ -162,6 +173,15 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
   const int nsub = g.nsub;
   const int n = C * M;
   const bool elem_fast = (elem_st == 1);
+  if (elem_fast && nsub == 1 && lines.pitch(LOAD) == M && g.scale == 1.0) {
+    // back-to-back lines: the tile is one contiguous range of global memory
+    const int64_t base = (LOAD ? lines.in(s0) : lines.out(s0));
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+      if (LOAD) tile[spad(idx)] = gin[base + idx];
+      else gout[base + idx] = tile[spad(idx)];
+    }
+    return;
+  }
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
     int c, i;
     if (elem_fast) {
@@ -176,11 +196,11 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
     const int64_t sub = s - line * nsub;
     const int64_t a = (LOAD ? lines.in(line) : lines.out(line)) + sub * sub_st + (int64_t)i * elem_st;
     if (LOAD) {
-      tile[c * M + i] = gin[a];
+      tile[spad(c * M + i)] = gin[a];
     } else if (g.scale == 1.0) {
-      gout[a] = tile[c * M + i];
+      gout[a] = tile[spad(c * M + i)];
     } else {
-      const auto v = tile[c * M + i];
+      const auto v = tile[spad(c * M + i)];
       const T sc = (T)g.scale;
       gout[a] = P::mk(P::mul(v.x, sc), P::mul(v.y, sc));
     }
@@ -211,7 +231,7 @@ __device__ __forceinline__ void process_tile(const GroupDesc& g, const Lines& li
                                              int C, const typename Prec<T>::C* in,
                                              typename Prec<T>::C* out, typename Prec<T>::C* smem) {
   auto* A = smem;
-  auto* B = smem + (size_t)g.C * g.M;
+  auto* B = smem + padded_elems(g.C * g.M);
   copy_tile<T, true>(A, in, nullptr, g, lines, s0, C);
   __syncthreads();
   // second group: the sub-problem index within the line enters the twiddle index

@@ -26,6 +26,137 @@ group_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
   process_tile<float, FWD>(g, StridedLines{g.in_line, g.out_line}, s0, C, in, out, smem_f32);
 }
 
+// ---- bulk-async (TMA) staging ------------------------------------------------------------
+
+constexpr int kStages = 2;                 // tiles in flight per CTA besides the one computed
+constexpr uint32_t kSpinLimit = 1u << 22;  // bounded mbarrier polls (each poll may suspend)
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// One contiguous global -> shared copy by the bulk-copy (TMA) engine, completing on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+
+// Poll with an iteration limit; false if the phase did not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i)
+    if (mbar_test(bar, parity)) return true;
+  return false;
+}
+
+// Persistent binary32 kernel for back-to-back lines of one pass group: each CTA walks the
+// tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...; the bulk-copy engine prefetches kStages
+// tiles ahead into stage buffers (one mbarrier each) while the CTA runs the passes of the
+// current tile in two work buffers, so HBM reads overlap the arithmetic.  The first pass
+// reads the stage buffer directly, after which the buffer is refilled with a later tile.
+// A wait that gives up sets *status = 1, waits (bounded) for this CTA's copies in flight and
+// returns.
+template <bool FWD>
+__global__ void __launch_bounds__(kGroupThreads)
+stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __restrict__ out,
+                  int64_t lines, int* status) {
+  extern __shared__ __align__(128) float2 smem_f32s[];
+  __shared__ __align__(8) uint64_t bars[kStages];
+  const int M = g.M, CM = g.C * g.M;
+  float2* A = smem_f32s + kStages * CM;       // stage buffers unpadded (bulk-copy targets)
+  float2* B = A + padded_elems(CM);
+  const int64_t ntiles = (lines + g.C - 1) / g.C;
+  bool pending[kStages];
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int s, int64_t tile) {   // thread 0 only
+    const int64_t l0 = tile * g.C;
+    const int cnt = (int)min((int64_t)g.C, lines - l0);
+    const uint32_t bytes = (uint32_t)cnt * M * sizeof(float2);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(&bars[s], bytes);
+    bulk_load(smem_f32s + s * CM, in + l0 * M, bytes, &bars[s]);
+  };
+  for (int s = 0; s < kStages; ++s) {
+    const int64_t t = blockIdx.x + (int64_t)s * gridDim.x;
+    pending[s] = t < ntiles;
+    if (threadIdx.x == 0 && pending[s]) issue(s, t);
+  }
+  uint32_t parity = 0;   // bit s: parity of stage s's next phase
+  int s = 0;
+  bool failed = false;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t l0 = tile * g.C;
+    const int C = (int)min((int64_t)g.C, lines - l0);
+    const bool ok = __syncthreads_and(mbar_wait(&bars[s], (parity >> s) & 1));
+    if (!ok) {
+      failed = true;
+      break;
+    }
+    parity ^= 1u << s;
+    pending[s] = false;
+    float2* src = smem_f32s + s * CM;
+    float2* dst = A;
+    for (int t = 0; t < g.npass; ++t) {
+      if (t == 0) run_pass_t<float, FWD, false>(src, dst, C, M, g.pass[t], g.kmul, -1, g.nsub);
+      else run_pass_t<float, FWD>(src, dst, C, M, g.pass[t], g.kmul, -1, g.nsub);
+      __syncthreads();
+      if (t == 0) {
+        // the stage buffer has been read: refill it with this CTA's tile kStages ahead
+        const int64_t next = tile + (int64_t)kStages * gridDim.x;
+        pending[s] = next < ntiles;
+        if (threadIdx.x == 0 && pending[s]) issue(s, next);
+        src = A;
+        dst = B;
+      } else {
+        float2* tmp = src;
+        src = dst;
+        dst = tmp;
+      }
+    }
+    // store the tile (contiguous): two complex values per 16-byte store
+    float4* o4 = reinterpret_cast<float4*>(out + l0 * M);
+    const int n4 = C * M / 2;
+    const float sc = (float)g.scale;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+      const float2 a = src[spad(2 * i)], b = src[spad(2 * i + 1)];
+      if (g.scale == 1.0) o4[i] = make_float4(a.x, a.y, b.x, b.y);
+      else o4[i] = make_float4(__fmul_rn(a.x, sc), __fmul_rn(a.y, sc), __fmul_rn(b.x, sc), __fmul_rn(b.y, sc));
+    }
+    __syncthreads();
+    s = (s + 1) % kStages;
+  }
+  if (failed) {
+    if (threadIdx.x == 0) atomicExch(status, 1);
+    // let this CTA's own copies in flight land before the CTA (and its smem) goes away
+    for (int k = 0; k < kStages; ++k)
+      if (pending[k]) mbar_wait(&bars[k], (parity >> k) & 1);
+  }
+}
+
 template <class K>
 cudaError_t allow_max_smem(K kern) {
   cudaFuncAttributes a;
@@ -40,12 +171,35 @@ cudaError_t allow_max_smem(K kern) {
 cudaError_t prepare_group_kernels_f32() {
   cudaError_t e = allow_max_smem(group_kernel_f32<true>);
   if (e != cudaSuccess) return e;
-  return allow_max_smem(group_kernel_f32<false>);
+  if ((e = allow_max_smem(group_kernel_f32<false>)) != cudaSuccess) return e;
+  if ((e = allow_max_smem(stream_kernel_f32<true>)) != cudaSuccess) return e;
+  return allow_max_smem(stream_kernel_f32<false>);
+}
+
+size_t stream_smem_bytes_f32(const GroupDesc& g) {
+  return ((size_t)kStages * g.C * g.M + 2 * (size_t)padded_elems(g.C * g.M)) * sizeof(float2);
+}
+
+int stream_blocks_per_sm_f32(const GroupDesc& g) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_kernel_f32<true>, kGroupThreads,
+                                                    stream_smem_bytes_f32(g)) != cudaSuccess)
+    return 1;
+  return nb > 0 ? nb : 1;
+}
+
+cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
+                              int64_t lines, unsigned grid, int* status, cudaStream_t stream) {
+  if (lines <= 0) return cudaSuccess;
+  auto kern = fwd ? stream_kernel_f32<true> : stream_kernel_f32<false>;
+  kern<<<grid, kGroupThreads, stream_smem_bytes_f32(g), stream>>>(
+      g, static_cast<const float2*>(in), static_cast<float2*>(out), lines, status);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_group_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                              cudaStream_t stream) {
-  const size_t smem = 2 * (size_t)g.C * g.M * sizeof(float2);
+  const size_t smem = 2 * (size_t)padded_elems(g.C * g.M) * sizeof(float2);
   const int64_t grid = (g.total_sub + g.C - 1) / g.C;
   if (grid <= 0) return cudaSuccess;
   auto kern = fwd ? group_kernel_f32<true> : group_kernel_f32<false>;

@@ -43,6 +43,7 @@ struct FixedBases {
   int64_t in_base, out_base;
   __device__ int64_t in(int64_t) const { return in_base; }
   __device__ int64_t out(int64_t) const { return out_base; }
+  __device__ int64_t pitch(bool) const { return -1; }
 };
 
 template <bool FWD, int NT, int MINB>
@@ -98,7 +99,9 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
 
 }  // namespace
 
-size_t group_smem_bytes_f64(const GroupDesc& g) { return 2 * (size_t)g.C * g.M * sizeof(double2); }
+size_t group_smem_bytes_f64(const GroupDesc& g) {
+  return 2 * (size_t)padded_elems(g.C * g.M) * sizeof(double2);
+}
 
 size_t ragged_smem_bytes_f64(const RaggedClass& c) {
   size_t m = 0;

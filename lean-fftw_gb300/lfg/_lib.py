@@ -67,6 +67,7 @@ _SIG = {
     "lfg_execute": (ctypes.c_int, [_VP, _VP, _VP, _VP]),
     "lfg_execute_host": (ctypes.c_int, [_VP, _VP, _VP]),
     "lfg_destroy": (None, [_VP]),
+    "lfg_device_status": (ctypes.c_int, [_VP]),
     "lfg_get_plan_info": (ctypes.c_int, [_VP, ctypes.POINTER(PlanInfo)]),
     "lfg_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "lfg_last_error": (ctypes.c_char_p, []),

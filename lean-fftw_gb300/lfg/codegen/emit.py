@@ -120,26 +120,63 @@ def cuda_codelets(radices: List[int], fp32: bool = False) -> str:
 
 
 def c_codelets(radices: List[int]) -> str:
-    """C codelets for the CPU restatement of the reference transform, plus a lookup
-    function `lfo_codelet(fwd, R, tw)` returning the function pointer (NULL if absent).
+    """C codelets for the CPU restatement of the reference transform: per (direction, radix,
+    twiddling) a codelet `lfo_bf_*` and a whole Stockham pass `lfo_pass_*` with the codelet
+    inlined (the pass of lean-fftw `LeanFFTW/Gen/Stockham.lean:263-284`), plus lookups
+    `lfo_codelet(fwd, R, tw)` and `lfo_pass(fwd, R, tw)` (NULL if absent).
     Compile with -ffp-contract=off."""
     out = ["/* Generated by lfg/codegen/emit.py. Compile with -ffp-contract=off. */",
            "#include <math.h>", "#include <stddef.h>", "",
-           "typedef void (*lfo_codelet_fn)(const double *x, double *y);", ""]
+           "typedef void (*lfo_codelet_fn)(const double *x, double *y);",
+           "typedef void (*lfo_pass_fn)(long N, long ns, const double *tw, const double *z,",
+           "                            double *o);", ""]
     table = []
     for R in radices:
         for fwd in (True, False):
             for tw in (False, True):
                 k = butterfly_k(fwd, R, tw)
                 name = "lfo_" + codelet_name(fwd, R, tw)
-                out.append(f"static void {name}(const double *restrict x, double *restrict y) {{")
+                pname = name.replace("lfo_bf_", "lfo_pass_")
+                out.append(f"static inline __attribute__((always_inline)) void {name}("
+                           f"const double *restrict x, double *restrict y) {{")
                 out += ["  " + ln for ln in kernel_body(k, "c")]
                 out.append("}")
                 out.append("")
-                table.append((fwd, R, tw, name))
+                nx = 4 * R - 2 if tw else 2 * R
+                out += [
+                    f"static void {pname}(long N, long ns, const double *restrict tw, "
+                    f"const double *restrict z, double *restrict o) {{",
+                    f"  const long NR = N / {R};",
+                    "  for (long j = 0; j < NR; ++j) {",
+                    "    const long k = j % ns, b = j / ns;",
+                    f"    double x[{nx}], y[{2 * R}];",
+                    f"    for (int r = 0; r < {R}; ++r) {{",
+                    "      x[2 * r] = z[2 * (j + r * NR)];",
+                    "      x[2 * r + 1] = z[2 * (j + r * NR) + 1];",
+                    "    }",
+                ]
+                if tw:
+                    out += [f"    for (int r = 0; r < {R - 1}; ++r) {{",
+                            f"      x[{2 * R} + 2 * r] = tw[2 * r * ns + k];",
+                            f"      x[{2 * R} + 2 * r + 1] = tw[(2 * r + 1) * ns + k];",
+                            "    }"]
+                out += [f"    {name}(x, y);",
+                        f"    for (int r = 0; r < {R}; ++r) {{",
+                        f"      const long c = b * ns * {R} + k + r * ns;",
+                        "      o[2 * c] = y[2 * r];",
+                        "      o[2 * c + 1] = y[2 * r + 1];",
+                        "    }",
+                        "  }",
+                        "}", ""]
+                table.append((fwd, R, tw, name, pname))
     out.append("lfo_codelet_fn lfo_codelet(int fwd, int R, int tw) {")
-    for fwd, R, tw, name in table:
+    for fwd, R, tw, name, _ in table:
         out.append(f"  if (fwd == {int(fwd)} && R == {R} && tw == {int(tw)}) return {name};")
+    out.append("  return NULL;")
+    out.append("}")
+    out.append("lfo_pass_fn lfo_pass(int fwd, int R, int tw) {")
+    for fwd, R, tw, _, pname in table:
+        out.append(f"  if (fwd == {int(fwd)} && R == {R} && tw == {int(tw)}) return {pname};")
     out.append("  return NULL;")
     out.append("}")
     return "\n".join(out) + "\n"

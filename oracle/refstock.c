@@ -25,7 +25,9 @@
 #endif
 
 typedef void (*lfo_codelet_fn)(const double *x, double *y);
+typedef void (*lfo_pass_fn)(long N, long ns, const double *tw, const double *z, double *o);
 lfo_codelet_fn lfo_codelet(int fwd, int R, int tw);
+lfo_pass_fn lfo_pass(int fwd, int R, int tw);
 
 /* ------------------------------------------------------------------ 1. refTransform */
 
@@ -35,6 +37,11 @@ lfo_codelet_fn lfo_codelet(int fwd, int R, int tw);
 static int ref_pass(int fwd, long N, int R, long ns, const double *tw, const double *z,
                     double *o)
 {
+     lfo_pass_fn pf = lfo_pass(fwd, R, tw != NULL);
+     if (pf) {   /* the generated pass with the codelet inlined */
+          pf(N, ns, tw, z, o);
+          return 0;
+     }
      lfo_codelet_fn f = lfo_codelet(fwd, R, tw != NULL);
      double x[4 * 64], y[2 * 64];
      long NR = N / R, j;

@@ -25,6 +25,7 @@ def _run(n, B, x, sign=-1, compensated=True):
     xd = torch.from_numpy(x.astype(np.complex64)).cuda()
     y = plan.execute(xd)
     torch.cuda.synchronize()
+    assert lfg.lib().lfg_device_status(plan._h) == 0     # no bounded wait gave up
     return y.cpu().numpy().astype(np.complex128)
 
 
@@ -36,6 +37,25 @@ def test_fp32_error_per_size(n):
         y = _run(n, B, x, sign)
         e = O.rel_l2(y, O.dd_dft(sign < 0, x, nthreads=8))
         assert e < 4 * U32 * max(1.0, np.sqrt(np.log2(n))), (n, sign, e)
+
+
+def test_fp32_inplace_and_unaligned():
+    """The persistent bulk-copy kernel runs in place; a buffer offset by one complex value
+    (8 bytes, not 16-byte aligned) takes the other kernel; both agree."""
+    n, B = 1024, 37
+    x = O.uniform_complex((B + 1, n), seed=3).astype(np.complex64)
+    plan = lfg.plan_1d(n, -1, B, precision="f32")
+    a = torch.from_numpy(x[:B].copy()).cuda()
+    ref = plan.execute(a.clone())
+    plan.execute(a, a)                                   # in place
+    buf = torch.from_numpy(x.reshape(-1)).cuda()
+    un_in = buf[1: 1 + B * n]                            # 8-byte offset
+    un_out = torch.empty(B * n + 1, dtype=torch.complex64, device="cuda")[1:]
+    plan.execute(un_in, un_out)
+    torch.cuda.synchronize()
+    assert torch.equal(a, ref)
+    shifted = torch.from_numpy(x.reshape(-1)[1: 1 + B * n].reshape(B, n)).cuda()
+    assert torch.equal(un_out.view(B, n), plan.execute(shifted))
 
 
 @pytest.mark.parametrize("n", [1 << 16, 1 << 17, 1 << 18])
