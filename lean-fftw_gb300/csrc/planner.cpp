@@ -165,6 +165,9 @@ void fill_group(GroupDesc& g, const std::vector<int>& rs, const PassTables& pt, 
   g.npass = t1 - t0;
   g.nsub = (int)nsub;
   int64_t cmax = std::max<int64_t>(1, tile_target / M);
+  // strided sub-problems are copied as runs of C neighbouring elements: keep the binary32
+  // runs at 64 bytes or more (two 32-byte sectors), which HBM serves at full rate
+  if (precision == 1 && nsub > 1) cmax = std::max<int64_t>(cmax, 8);
   while (cmax > 1 && smem_bytes(cmax, M, precision) > kSmemBudget) --cmax;
   // tiles may straddle lines (the sub-problem index is taken per element), so C need not
   // divide nsub; prefer a divisor when one is close to the target

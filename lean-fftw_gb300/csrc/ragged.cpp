@@ -161,6 +161,8 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
     if (cudaMalloc(d, std::max<size_t>(bytes, 16)) != cudaSuccess) return false;
     return bytes == 0 || cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
   };
+  for (RaggedClass& rc : r.classes_host)
+    for (int gi = 0; gi < rc.ngroups; ++gi) set_divisors(rc.g[gi]);
   if (!up(&r.d_classes, r.classes_host.data(), r.classes_host.size() * sizeof(RaggedClass)) ||
       !up(&r.d_items, r.items_host.data(), r.items_host.size() * sizeof(RaggedItem)) ||
       !up(&r.d_in_off, in_sorted.data(), in_sorted.size() * sizeof(int64_t)) ||

@@ -132,8 +132,10 @@ cudaError_t prepare_real_kernels_f64() {
   return allow_max_smem(c2r_kernel_f64);
 }
 
-cudaError_t launch_real_f64(const RealDesc& d, bool r2c, const void* in, void* out,
+cudaError_t launch_real_f64(const RealDesc& rd, bool r2c, const void* in, void* out,
                             cudaStream_t stream) {
+  RealDesc d = rd;
+  set_divisors(d.g);
   const int64_t grid = (d.lines + d.g.C - 1) / d.g.C;
   if (grid <= 0) return cudaSuccess;
   const size_t smem = 2 * (size_t)padded_elems(d.g.C * d.M) * sizeof(double2);

@@ -30,6 +30,30 @@ namespace lfg {
 constexpr int kMaxPass = 24;       // lean-fftw Asm/Planner.lean:49 (`maxPass`)
 constexpr int kMaxRadix = 16;
 
+// Division of 0 <= n < 2^31 by a divisor d >= 1 fixed at plan time, as one multiply-high, an
+// add and a shift: q = (umulhi(m, n) + n) >> l with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1 (Granlund and Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994, Fig. 4.1, specialised to 31-bit dividends so that the sum
+// cannot overflow).  The kernels' index arithmetic divides by sub-problem lengths, tile sizes
+// and pass strides that only the plan knows.
+struct FastDiv {
+  uint32_t m;
+  uint32_t l;
+};
+
+inline FastDiv make_fastdiv(int d) {
+  uint32_t l = 0;
+  while (l < 31 && (1u << l) < (uint32_t)d) ++l;
+  const uint64_t m = ((uint64_t(1) << 32) * ((uint64_t(1) << l) - (uint64_t)d)) / (uint64_t)d + 1;
+  return FastDiv{(uint32_t)m, l};
+}
+
+// Host-side evaluation of the same formula (tests, planner checks).
+inline int fastdiv_host(int n, FastDiv f) {
+  const uint32_t t = (uint32_t)(((uint64_t)f.m * (uint32_t)n) >> 32);
+  return (int)((t + (uint32_t)n) >> f.l);
+}
+
 struct PassDesc {
   int R;                 // radix of the pass
   int ns_loc;            // product of the group's earlier radices
@@ -37,6 +61,8 @@ struct PassDesc {
   int comp;              // binary32 only: twiddles as (hi, lo) pairs, compensated products
   const void* tw;        // pass twiddle table (2*(R-1)*ns_g scalars; binary32 comp passes:
                          // the hi table followed by the lo table), nullptr for pass 0
+  FastDiv fd_mr;         // divisor M / R (butterflies per sub-problem)
+  FastDiv fd_ns;         // divisor ns_loc
 };
 
 // Complex element (s, i) of sub-problem s (flattened over lines) lives at
@@ -53,8 +79,22 @@ struct GroupDesc {
   int kmul;              // table index k = k_loc * kmul + (twsub ? s % nsub : 0)
   int twsub;
   double scale;          // outputs multiplied by this on store unless it is exactly 1
+  FastDiv fd_m, fd_c, fd_nsub;   // divisors M, C, nsub (set_divisors)
   PassDesc pass[kMaxPass];
 };
+
+// Fill the FastDiv fields from M, C, nsub and the passes; every launch path calls this on
+// the descriptor it passes to a kernel, so planners may change C freely before.
+inline void set_divisors(GroupDesc& g) {
+  g.fd_m = make_fastdiv(g.M > 0 ? g.M : 1);
+  g.fd_c = make_fastdiv(g.C > 0 ? g.C : 1);
+  g.fd_nsub = make_fastdiv(g.nsub > 0 ? g.nsub : 1);
+  for (int t = 0; t < g.npass && t < kMaxPass; ++t) {
+    PassDesc& d = g.pass[t];
+    d.fd_mr = make_fastdiv(d.R > 0 ? g.M / d.R : 1);
+    d.fd_ns = make_fastdiv(d.ns_loc > 0 ? d.ns_loc : 1);
+  }
+}
 
 // One distinct size of a ragged batch: one group, or two groups run back to back by one CTA
 // (first group to the output, second group in place on the output).  Line strides of the

@@ -48,14 +48,21 @@ struct Prec<float> {
 __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int padded_elems(int n) { return n + (n >> 4) + 1; }
 
+// n / d for 0 <= n < 2^31 with the plan's FastDiv of d (stockham.h).
+__device__ __forceinline__ int fdiv(int n, const FastDiv& f) {
+  return (int)((__umulhi(f.m, (unsigned)n) + (unsigned)n) >> f.l);
+}
+
 // One pass over the C sub-problems of a tile: src, dst are tile buffers in shared memory
 // (dst padded; src padded unless SRCPAD is false, as for a stage buffer a bulk copy filled).
 // MODE 0: untwiddled; 1: twiddled codelet (table twiddles); 2: compensated twiddle products
 // with (hi, lo) binary32 twiddles, then the untwiddled codelet.
+// sub0: index within its line of the tile's first sub-problem (second group), else -1.
 template <class T, bool FWD, int R, int MODE, bool SRCPAD = true>
 __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ src,
                                        typename Prec<T>::C* __restrict__ dst, int C, int M,
-                                       const PassDesc& pd, int kmul, int64_t msub0, int nsub) {
+                                       const PassDesc& pd, int kmul, int sub0, int nsub,
+                                       const FastDiv& fd_nsub) {
   using P = Prec<T>;
   using Cx = typename P::C;
   constexpr bool TW = MODE == 1;
@@ -64,8 +71,9 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
   const int ns = pd.ns_loc;
   const T* __restrict__ tw = static_cast<const T*>(pd.tw);
   const int64_t nsg = pd.ns_g;
+  const FastDiv fd_mr = pd.fd_mr, fd_ns = pd.fd_ns;
   for (int q = threadIdx.x; q < nb; q += blockDim.x) {
-    const int c = q / MR;
+    const int c = fdiv(q, fd_mr);
     const int j = q - c * MR;
     T x[TW ? 4 * R - 2 : 2 * R];
     T y[2 * R];
@@ -77,10 +85,16 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
       x[2 * r] = v.x;
       x[2 * r + 1] = v.y;
     }
-    const int k = j % ns;
-    // table index of the twiddle: k_loc * kmul + sub-problem index (second group only)
-    // (msub0 >= 0: first sub-problem of the tile, flattened over lines; tiles may straddle lines)
-    const int64_t kg = (int64_t)k * kmul + (msub0 >= 0 ? (msub0 + c) % nsub : 0);
+    const int b = fdiv(j, fd_ns);
+    const int k = j - b * ns;
+    // table index of the twiddle: k_loc * kmul + sub-problem index within the line (second
+    // group only; tiles may straddle lines, so the index wraps at nsub)
+    int msub = 0;
+    if (sub0 >= 0) {
+      const int t = sub0 + c;
+      msub = t - fdiv(t, fd_nsub) * nsub;
+    }
+    const int64_t kg = (int64_t)k * kmul + msub;
     if (MODE == 1) {
 #pragma unroll
       for (int r = 0; r < R - 1; ++r) {
@@ -102,7 +116,6 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
       }
     }
     P::template Bfly<FWD, R, TW>::run(x, y);
-    const int b = j / ns;
     const int d0 = c * M + b * ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) dst[spad(d0 + r * ns)] = P::mk(y[2 * r], y[2 * r + 1]);
@@ -112,12 +125,13 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
 template <class T, bool FWD, bool SRCPAD = true>
 __device__ __forceinline__ void run_pass_t(const typename Prec<T>::C* src, typename Prec<T>::C* dst,
                                            int C, int M, const PassDesc& pd, int kmul,
-                                           int64_t msub0, int nsub) {
+                                           int sub0, int nsub, const FastDiv& fd_nsub) {
 #define LFG_PASS_CASE(RR)                                                                        \
   case RR:                                                                                       \
-    if (!pd.tw) pass_t<T, FWD, RR, 0, SRCPAD>(src, dst, C, M, pd, kmul, msub0, nsub);            \
-    else if (sizeof(T) == 4 && pd.comp) pass_t<T, FWD, RR, 2, SRCPAD>(src, dst, C, M, pd, kmul, msub0, nsub); \
-    else pass_t<T, FWD, RR, 1, SRCPAD>(src, dst, C, M, pd, kmul, msub0, nsub);                   \
+    if (!pd.tw) pass_t<T, FWD, RR, 0, SRCPAD>(src, dst, C, M, pd, kmul, sub0, nsub, fd_nsub);    \
+    else if (sizeof(T) == 4 && pd.comp)                                                          \
+      pass_t<T, FWD, RR, 2, SRCPAD>(src, dst, C, M, pd, kmul, sub0, nsub, fd_nsub);              \
+    else pass_t<T, FWD, RR, 1, SRCPAD>(src, dst, C, M, pd, kmul, sub0, nsub, fd_nsub);           \
     break;
   switch (pd.R) {
     LFG_PASS_CASE(2)
@@ -182,18 +196,26 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
     }
     return;
   }
-  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+  // line and in-line index of the tile's first sub-problem (one 64-bit division per tile)
+  const int64_t line0 = s0 / nsub;
+  const int sub0 = (int)(s0 - line0 * nsub);
+  // strided sub-problems: neighbouring threads take neighbouring sub-problems, over the full
+  // tile width g.C (a partial last tile skips the missing columns)
+  const int nn = elem_fast ? n : g.C * M;
+  for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
     int c, i;
     if (elem_fast) {
-      c = idx / M;
+      c = fdiv(idx, g.fd_m);
       i = idx - c * M;
     } else {
-      i = idx / C;
-      c = idx - i * C;
+      i = fdiv(idx, g.fd_c);
+      c = idx - i * g.C;
+      if (c >= C) continue;
     }
-    const int64_t s = s0 + c;
-    const int64_t line = s / nsub;
-    const int64_t sub = s - line * nsub;
+    const int t = sub0 + c;
+    const int ql = fdiv(t, g.fd_nsub);
+    const int64_t line = line0 + ql;
+    const int64_t sub = t - ql * nsub;
     const int64_t a = (LOAD ? lines.in(line) : lines.out(line)) + sub * sub_st + (int64_t)i * elem_st;
     if (LOAD) {
       tile[spad(c * M + i)] = gin[a];
@@ -215,8 +237,10 @@ __device__ __forceinline__ typename Prec<T>::C* run_passes(const GroupDesc& g,
                                                            typename Prec<T>::C* B, int C,
                                                            int64_t msub0) {
   const int npass = g.npass;
+  const int sub0 = msub0 >= 0 ? (int)(msub0 % g.nsub) : -1;
+  const FastDiv fd_nsub = g.fd_nsub;
   for (int t = 0; t < npass; ++t) {
-    run_pass_t<T, FWD>(A, B, C, g.M, g.pass[t], g.kmul, msub0, g.nsub);
+    run_pass_t<T, FWD>(A, B, C, g.M, g.pass[t], g.kmul, sub0, g.nsub, fd_nsub);
     __syncthreads();
     auto tmp = A;
     A = B;

@@ -121,8 +121,8 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
     float2* src = smem_f32s + s * CM;
     float2* dst = A;
     for (int t = 0; t < g.npass; ++t) {
-      if (t == 0) run_pass_t<float, FWD, false>(src, dst, C, M, g.pass[t], g.kmul, -1, g.nsub);
-      else run_pass_t<float, FWD>(src, dst, C, M, g.pass[t], g.kmul, -1, g.nsub);
+      if (t == 0) run_pass_t<float, FWD, false>(src, dst, C, M, g.pass[t], g.kmul, -1, g.nsub, g.fd_nsub);
+      else run_pass_t<float, FWD>(src, dst, C, M, g.pass[t], g.kmul, -1, g.nsub, g.fd_nsub);
       __syncthreads();
       if (t == 0) {
         // the stage buffer has been read: refill it with this CTA's tile kStages ahead
@@ -188,8 +188,10 @@ int stream_blocks_per_sm_f32(const GroupDesc& g) {
   return nb > 0 ? nb : 1;
 }
 
-cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
+cudaError_t launch_stream_f32(const GroupDesc& gd, bool fwd, const void* in, void* out,
                               int64_t lines, unsigned grid, int* status, cudaStream_t stream) {
+  GroupDesc g = gd;
+  set_divisors(g);
   if (lines <= 0) return cudaSuccess;
   auto kern = fwd ? stream_kernel_f32<true> : stream_kernel_f32<false>;
   kern<<<grid, kGroupThreads, stream_smem_bytes_f32(g), stream>>>(
@@ -197,8 +199,10 @@ cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void
   return cudaGetLastError();
 }
 
-cudaError_t launch_group_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
+cudaError_t launch_group_f32(const GroupDesc& gd, bool fwd, const void* in, void* out,
                              cudaStream_t stream) {
+  GroupDesc g = gd;
+  set_divisors(g);
   const size_t smem = 2 * (size_t)padded_elems(g.C * g.M) * sizeof(float2);
   const int64_t grid = (g.total_sub + g.C - 1) / g.C;
   if (grid <= 0) return cudaSuccess;

@@ -177,8 +177,10 @@ cudaError_t prepare_group_kernels_f64() {
   return cudaSuccess;
 }
 
-cudaError_t launch_group_f64(const GroupDesc& g, bool fwd, const void* in, void* out,
+cudaError_t launch_group_f64(const GroupDesc& gd, bool fwd, const void* in, void* out,
                              cudaStream_t stream) {
+  GroupDesc g = gd;
+  set_divisors(g);
   const size_t smem = group_smem_bytes_f64(g);
   const int64_t grid = (g.total_sub + g.C - 1) / g.C;
   if (grid <= 0) return cudaSuccess;
