@@ -15,6 +15,8 @@ Workloads (synthetic inputs, re/im iid uniform[-0.5, 0.5) from numpy default_rng
   large_262144[_f32]  32 transforms of N = 2^18, binary64 (or binary32: the FP32 variant with
              compensated last-pass twiddles).
   c2c_1024_f32  the binary32 variant at N = 1024, batch 2^17 (1 GiB in and out).
+  r2c_512x512[_f32]  64 real 512 x 512 images to 64 x 512 x 257 half spectra (fused r2c
+             rows, then the column transforms in place); GFLOP/s counts 2.5 N log2 N per image.
   grad_4096  differentiation: batch 256 x N = 4096, loss = sum |W * FFT(x)|^2 (W iid complex
              normal), one forward transform and one adjoint transform (the backward pass) per
              step through torch.autograd; GFLOP/s counts both transforms.
@@ -60,6 +62,9 @@ WORKLOADS.update({
     "c2c_1024_f32": dict(kind="c2c", n=1024, batch=1 << 17, sign=-1, precision="f32"),
     # differentiation: loss = sum |W * FFT(x)|^2, forward transform + adjoint per step
     "grad_4096": dict(kind="grad", n=4096, batch=256, sign=-1),
+    # large images: 64 real 512 x 512 images to 64 x 512 x 257 half spectra
+    "r2c_512x512": dict(kind="r2c2d", n0=512, n1=512, batch=64, sign=-1),
+    "r2c_512x512_f32": dict(kind="r2c2d", n0=512, n1=512, batch=64, sign=-1, precision="f32"),
 })
 
 
@@ -194,6 +199,15 @@ def cpu_reference(wl, steps, warmup, budget_s=None):
         call = lambda: runner.run(x, y, nthreads=threads)
         flops = float(sum(flops_per_transform(int(n)) for n in sizes))
         sample = f"the whole batch ({len(sizes)} transforms, {len(plans)} sizes) per timed call"
+    elif wl["kind"] == "r2c2d":
+        # lean-fftw runs rdft2 in its generic engine (Core/Problem.lean:222-236): restated
+        n0, n1 = wl["n0"], wl["n1"]
+        count = min(wl["batch"], max(1, threads // 2))
+        x = np.random.default_rng(SEED).random((count, n0, n1)) - 0.5
+        call = lambda: O.generic_rank2_r2c(x, nthreads=threads)
+        flops = 2.5 * n0 * n1 * math.log2(n0 * n1) * count
+        sample = (f"{count} of the {wl['batch']} images ({n0}x{n1}, binary64) per timed call "
+                  "through the generic engine's rdft2")
     else:
         n = wl["n"]
         rs = reference_plan(n)
@@ -238,10 +252,20 @@ def reference_plan(n):
 METRIC = "FP64 c2c FFT GFLOP/s (5 N log2 N)"
 
 
+def metric_name(wl):
+    m = METRIC
+    if wl["kind"] == "r2c2d":
+        m = "FP64 r2c FFT GFLOP/s (2.5 N log2 N)"
+    return m if wl.get("precision", "f64") == "f64" else m.replace("FP64", "FP32")
+
+
 def workload_config(name, wl):
     if wl["kind"] == "ragged":
         return {"workload": name, "transforms": wl["count"], "sizes": "13-smooth in [2, 16384], "
                 "log-uniform, seed 20261016", "sign": wl["sign"], "layout": "packed, size order"}
+    if wl["kind"] == "r2c2d":
+        return {"workload": name, "n0": wl["n0"], "n1": wl["n1"], "batch": wl["batch"],
+                "sign": wl["sign"]}
     return {"workload": name, "n": wl["n"], "batch": wl["batch"], "sign": wl["sign"]}
 
 
@@ -251,7 +275,7 @@ def run_reference(args, wl):
         return
     gf, threads, sample = cpu_reference(wl, max(1, args.steps), max(0, min(args.warmup, 2)),
                                         budget_s=60)
-    line = {"metric": METRIC, "value": round(gf, 3),
+    line = {"metric": metric_name(wl), "value": round(gf, 3),
             "unit": "GFLOP/s", "impl": "reference", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -340,6 +364,7 @@ def main():
     stream = torch.cuda.current_stream()
     rng = np.random.default_rng(rank_seed(rank))
     extra = {}
+    out_shape, out_dtype, alg_bytes_override = None, None, None
     if wl["kind"] == "ragged":
         sizes = ragged_workload_sizes(wl)
         total = int(sizes.sum())
@@ -356,6 +381,24 @@ def main():
         extra["config_extra"] = {"distinct_sizes": int(rinfo.classes), "points": total,
                                  "work_items": int(rinfo.items), "grid": int(rinfo.grid),
                                  "smem_bytes": int(rinfo.smem_bytes)}
+    elif wl["kind"] == "r2c2d":
+        n0, n1, B = wl["n0"], wl["n1"], wl["batch"]
+        prec = wl.get("precision", "f64")
+        rdt = np.float32 if prec == "f32" else np.float64
+        plan = lfg.plan_r2c_2d(n0, n1, B, precision=prec)
+        info = plan.info()
+        host = (rng.random((B, n0, n1)) - 0.5).astype(rdt)
+        out_shape = (B, n0, n1 // 2 + 1)
+        out_dtype = torch.complex64 if prec == "f32" else torch.complex128
+        flops_step = 2.5 * n0 * n1 * math.log2(n0 * n1) * B      # half a complex transform
+        launches_per_step = 2                                      # rows (fused r2c), columns
+        codelet_ops = info.flops
+        step_fn = lambda: plan.execute(x, y)
+        host_fn = lambda a, b: plan.execute_host(a, b)
+        esz_r = 4 if prec == "f32" else 8
+        alg_bytes_override = B * (n0 * n1 * esz_r + n0 * (n1 // 2 + 1) * 2 * esz_r)
+        points = n0 * n1 * B
+        extra["config_extra"] = {"images": B, "shape": [n0, n1], "radices": plan.radices}
     elif wl["kind"] == "grad":
         from lfg import torch_ops
         n, B = wl["n"], wl["batch"]
@@ -398,7 +441,7 @@ def main():
         host_fn = lambda a, b: plan.execute_host(a, b)
         extra["config_extra"] = {"radices": [info.radices[i] for i in range(info.npass)]}
     x = torch.from_numpy(host).to(dev)
-    y = torch.empty_like(x)
+    y = torch.empty(out_shape, dtype=out_dtype, device=dev) if out_shape else torch.empty_like(x)
     for _ in range(max(3, args.warmup)):
         step_fn()
     torch.cuda.synchronize()
@@ -428,6 +471,8 @@ def main():
     # roofline of the dominant kernel (one launch per step for ragged and single-group sizes)
     esz = 8.0 if wl.get("precision") == "f32" else 16.0
     alg_bytes = 2 * esz * points         # read + write of the data once
+    if alg_bytes_override is not None:   # real input, half-spectrum output
+        alg_bytes = float(alg_bytes_override)
     hbm_peak, peak_kind = peaks()
     kernel_ms = ms / launches_per_step
     achieved = alg_bytes / launches_per_step / (kernel_ms * 1e-3) / 1e9
@@ -436,7 +481,7 @@ def main():
 
     # end to end through the C ABI's host-pointer entry point (pinned host buffers)
     hin = torch.from_numpy(host).pin_memory()
-    hout = torch.empty_like(hin).pin_memory()
+    hout = torch.empty(tuple(y.shape), dtype=y.dtype).pin_memory()
     hin_np, hout_np = hin.numpy(), hout.numpy()
     host_fn(hin_np, hout_np)
     e2e_steps = max(2, min(args.steps, 10))
@@ -459,7 +504,7 @@ def main():
         config["l2_flush"] = ("inputs larger than L2 (129 MB)" if flush is None else
                               "L2 flushed before every timed step (258 MB write, not timed)")
         config["parallelism"] = f"replicas{ws}"
-        metric = METRIC if wl.get("precision", "f64") == "f64" else METRIC.replace("FP64", "FP32")
+        metric = metric_name(wl)
         line = {
             "metric": metric, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),

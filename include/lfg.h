@@ -46,7 +46,8 @@ typedef struct lfg_plan lfg_plan;
  *   [kind, sign, rank, vrank, inRe, inIm, outRe, outIm,
  *    (n, is, os) x rank, (n, is, os) x vrank, r2rkind x rank]
  * kind 0 = complex DFT, 1 = rdft2 (r2c when sign < 0, c2r otherwise); strides and offsets
- * are in doubles, relative to the pointers later given to lfg_execute.  Replaces
+ * are in real scalars of the plan's precision (doubles for LFG_F64, as in the reference;
+ * floats for LFG_F32), relative to the pointers later given to lfg_execute.  Replaces
  * `lfftw_generic_plan` (LeanFFTW/FFI.lean:50-52) for the kinds and layouts this library
  * executes.  A vector dimension of size 0 gives an empty plan (Core/Problem.lean:251-256).
  * Returns LFG_ERR_UNSUPPORTED (and *out = NULL) for anything else. */
@@ -67,8 +68,8 @@ lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision
                                const int *radices, int npass, lfg_plan **out);
 
 /* Real-input forward (r2c) and real-output backward (c2r) transforms, even n (13-smooth),
- * `howmany` contiguous lines: real lines of n doubles, complex lines of n/2+1 interleaved
- * values.  The rank-2 versions transform n0 x n1 images (r2c along the last axis, then a
+ * `howmany` contiguous lines: real lines of n scalars (double or float by `precision`),
+ * complex lines of n/2+1 interleaved values.  The rank-2 versions transform n0 x n1 images (r2c along the last axis, then a
  * complex DFT along the first; c2r the reverse), images contiguous.  Replaces the generic
  * engine's rdft2 path (`planProblemCore`, LeanFFTW/Core/Problem.lean:222-236, and
  * `LineOp.apply`, :142-150); c2r ignores the imaginary parts of the self-conjugate bins

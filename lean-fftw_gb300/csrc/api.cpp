@@ -134,7 +134,7 @@ lfg_status finish_real(lfg::Plan& p, const lfg::RealLayout& L, lfg_plan** out) {
   p.out_span = r2c ? cspan : rspan;
   if (!p.empty) {
     if ((e = lfg::prepare_group_kernels_f64()) != cudaSuccess) return cuda_fail(e, "kernel set-up");
-    if ((e = lfg::prepare_real_kernels_f64()) != cudaSuccess) return cuda_fail(e, "kernel set-up");
+    if ((e = lfg::prepare_real_kernels()) != cudaSuccess) return cuda_fail(e, "kernel set-up");
     std::string msg = lfg::build_real(p, L, tile_target());
     if (!msg.empty()) {
       lfg::free_plan_memory(p);
@@ -155,7 +155,7 @@ lfg_status plan_real_common(bool r2c, size_t n0, size_t n, size_t howmany, lfg_p
                             unsigned flags, lfg_plan** out) {
   if (!out) return fail(LFG_ERR_INVALID, "null output handle");
   *out = nullptr;
-  if (precision != LFG_F64) return fail(LFG_ERR_UNSUPPORTED, "precision not supported yet");
+  if (precision != LFG_F64 && precision != LFG_F32) return fail(LFG_ERR_INVALID, "bad precision");
   if (n < 2 || n0 < 1) return fail(LFG_ERR_UNSUPPORTED, "sizes must be >= 2 (last) and >= 1");
   if (!smooth13((int64_t)n) || !smooth13((int64_t)n0))
     return fail(LFG_ERR_UNSUPPORTED, "sizes must be 13-smooth");
@@ -264,7 +264,8 @@ lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precisi
     *is = (int64_t)spec[9 + 3 * i];
     *os = (int64_t)spec[10 + 3 * i];
   };
-  if (precision != LFG_F64) return fail(LFG_ERR_UNSUPPORTED, "precision not supported yet");
+  // offsets and strides count real scalars of the plan's precision (doubles or floats)
+  if (precision != LFG_F64 && precision != LFG_F32) return fail(LFG_ERR_INVALID, "bad precision");
   if (kind == 1) {
     // rdft2 (Core/Problem.lean:222-236): r2c when sign < 0 (real input), else c2r; the last
     // dimension is halved on the complex side.  Executed: rank 1 or 2, vector rank <= 1, unit

@@ -30,6 +30,13 @@ int stream_blocks_per_sm_f32(const GroupDesc& g);
 cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                               int64_t lines, unsigned grid, int* status, cudaStream_t stream);
 
+// Persistent FP32 kernel for tiles of strided sub-problems (three tile buffers: a stage
+// filled by asynchronous element copies, two work buffers); in and out 8-byte aligned.
+size_t tile_stream_smem_bytes_f32(const GroupDesc& g);
+int tile_stream_blocks_per_sm_f32(const GroupDesc& g);
+cudaError_t launch_tile_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
+                                   unsigned grid, cudaStream_t stream);
+
 // Persistent FP64 kernel over a ragged batch (one launch for all sizes), in kRaggedVariants
 // block shapes (threads x minimum CTAs per SM).
 constexpr int kRaggedVariants = 5;

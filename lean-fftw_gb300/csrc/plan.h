@@ -50,6 +50,10 @@ struct Plan {
   // binary32 single-group plans over back-to-back lines run the persistent bulk-copy kernel
   bool stream = false;
   unsigned stream_grid = 0;
+  // binary32 groups not covered by the stream kernel: the persistent strided-tile kernel
+  // (asynchronous copies of the next tile), one grid per group
+  bool tile_stream = false;
+  unsigned ts_grid[2] = {0, 0};
   int* d_status = nullptr; // set to 1 on the device when a bounded wait gave up
   // real transforms (kind R2C / C2R): rows of the last dimension, and for rank 2 the complex
   // transform along the first dimension (columns of the half spectrum)
@@ -90,6 +94,12 @@ struct PassTables {
   std::vector<int64_t> ns;
 };
 PassTables make_pass_tables(int64_t N, bool fwd, const std::vector<int>& rs, int precision);
+// Store the tables of passes split..end (the second pass group) transposed: within each row
+// of ns_g = ns_loc * P values, entry k_loc * P + m moves to m * ns_loc + k_loc, so that the
+// threads of a warp, which walk k_loc within one sub-problem m, read consecutive twiddles.
+// `comp` marks binary32 passes whose rows come as [hi rows | lo rows] (split_compensated).
+void transpose_second_group(PassTables& pt, const std::vector<int>& rs, int split,
+                            const std::vector<int>& comp);
 
 bool radix_ok(int R);
 std::string check_radices(int64_t N, const std::vector<int>& rs);

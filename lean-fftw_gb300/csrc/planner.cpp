@@ -71,9 +71,8 @@ int64_t divisor_at_most(int64_t n, int64_t cap) {
 }
 
 size_t smem_bytes(int64_t C, int64_t M, int precision) {
-  // two tile buffers, each padded by one element per 16 (stockham_dev.cuh: padded_elems)
-  const int64_t n = C * M;
-  return 2 * (size_t)(n + (n >> 4) + 1) * (precision == 0 ? 16 : 8);
+  // two tile buffers of C sub-problems, sub_pitch(M) elements apart (stockham.h)
+  return 2 * (size_t)tile_elems(C, (int)M) * (precision == 0 ? 16 : 8);
 }
 
 std::vector<int> choose_radices(int64_t n, int precision) {
@@ -140,6 +139,26 @@ PassTables make_pass_tables(int64_t N, bool fwd, const std::vector<int>& rs, int
     pass_twiddles(tab, fwd, (uint64_t)N, rs[t], (uint64_t)pt.ns[t], pt.values.data() + pt.offset[t]);
   (void)precision;
   return pt;
+}
+
+void transpose_second_group(PassTables& pt, const std::vector<int>& rs, int split,
+                            const std::vector<int>& comp) {
+  if (split <= 0 || split >= (int)rs.size()) return;
+  int64_t P = 1;
+  for (int t = 0; t < split; ++t) P *= rs[t];
+  std::vector<double> row;
+  for (int t = split; t < (int)rs.size(); ++t) {
+    if (t == 0) continue;
+    const int64_t ns = pt.ns[t], nl = ns / P;
+    const int rows = 2 * (rs[t] - 1) * (!comp.empty() && comp[t] ? 2 : 1);
+    row.resize((size_t)ns);
+    for (int q = 0; q < rows; ++q) {
+      double* v = pt.values.data() + pt.offset[t] + (size_t)q * ns;
+      for (int64_t k = 0; k < nl; ++k)
+        for (int64_t m = 0; m < P; ++m) row[(size_t)(m * nl + k)] = v[k * P + m];
+      std::copy(row.begin(), row.end(), v);
+    }
+  }
 }
 
 int split_point(int64_t N, const std::vector<int>& rs, int64_t max_m) {
@@ -288,6 +307,7 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   PassTables pt = make_pass_tables(N, p.fwd, rs, prec);
   const std::vector<int> comp = compensated_passes(N, rs, split, p.no_comp ? 0 : prec);
   if (prec == 1) pt.values = split_compensated(pt, rs, comp);
+  transpose_second_group(pt, rs, split, comp);
   p.d_twiddles = upload_tables(pt.values, prec, &msg);
   if (!p.d_twiddles) return msg;
 
@@ -350,6 +370,27 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
       p.stream = true;
     }
   }
+  if (prec == 1 && !p.stream && p.howmany > 0) {
+    // three tile buffers per CTA (stage + two work buffers): shrink C to fit
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    bool fits = true;
+    for (int gi = 0; gi < p.ngroups; ++gi) {
+      GroupDesc& g = p.groups[gi];
+      while (g.C > 1 && smem_bytes(g.C, g.M, prec) / 2 * 3 > kSmemBudget) --g.C;
+      if (smem_bytes(g.C, g.M, prec) / 2 * 3 > kSmemBudget) fits = false;
+    }
+    if (fits) {
+      for (int gi = 0; gi < p.ngroups; ++gi) {
+        const GroupDesc& g = p.groups[gi];
+        const int64_t tiles = (g.total_sub + g.C - 1) / g.C;
+        const int64_t want = (int64_t)sms * tile_stream_blocks_per_sm_f32(g);
+        p.ts_grid[gi] = (unsigned)std::max<int64_t>(1, std::min(want, tiles));
+      }
+      p.tile_stream = true;
+    }
+  }
   return "";
 }
 
@@ -409,7 +450,8 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
   p.d_post = upload_tables(post, prec, &msg);
   if (!p.d_post) return msg;
   d.post = p.d_post;
-  d.post_full = (const double*)p.d_post + 2 * np;
+  d.post_full = prec == 0 ? (const void*)((const double*)p.d_post + 2 * np)
+                          : (const void*)((const float*)p.d_post + 2 * np);
   p.flops = (plan_ops(M, p.radices) + 6.0 * M) * (double)d.lines;
   // rank 2: complex transform of length n0 along the first axis of the half spectrum
   p.has_col = L.n0 > 1;
@@ -443,7 +485,7 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
       p.col_in_off = L.c_off;
       d.c_off = 0;
       // the column transform's output, allocated with the plan
-      const size_t need = (size_t)L.howmany * L.n0 * h * 16;
+      const size_t need = (size_t)L.howmany * L.n0 * h * (prec == 0 ? 16 : 8);
       if (cudaMalloc(&p.d_scratch, need) != cudaSuccess) return "cudaMalloc of the c2r scratch failed";
       p.scratch_bytes = need;
       d.c_bdist = L.n0 * h;
@@ -457,25 +499,30 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
 cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream,
                          bool force_scratch) {
   if (p.empty) return cudaSuccess;
+  const size_t es = p.precision == 0 ? 16 : 8;
+  auto launch_col = [&](bool fwd, const void* a, void* b) -> cudaError_t {
+    if (p.precision == 0) return launch_group_f64(p.col, fwd, a, b, stream);
+    return launch_group_f32(p.col, fwd, a, b, stream);
+  };
   if (p.kind == Kind::R2C) {
-    cudaError_t e = launch_real_f64(p.real, true, in, out, stream);
+    cudaError_t e = launch_real(p.real, p.precision, true, in, out, stream);
     if (e != cudaSuccess || !p.has_col) return e;
-    const size_t es = 16;
     char* ob = static_cast<char*>(out) + p.real.c_off * (int64_t)es;
-    return launch_group_f64(p.col, true, ob, ob, stream);
+    return launch_col(true, ob, ob);
   }
   if (p.kind == Kind::C2R) {
-    if (!p.has_col) return launch_real_f64(p.real, false, in, out, stream);
-    const char* ib = static_cast<const char*>(in) + p.col_in_off * 16;
-    cudaError_t e = launch_group_f64(p.col, false, ib, p.d_scratch, stream);
+    if (!p.has_col) return launch_real(p.real, p.precision, false, in, out, stream);
+    const char* ib = static_cast<const char*>(in) + p.col_in_off * (int64_t)es;
+    cudaError_t e = launch_col(false, ib, p.d_scratch);
     if (e != cudaSuccess) return e;
-    return launch_real_f64(p.real, false, p.d_scratch, out, stream);
+    return launch_real(p.real, p.precision, false, p.d_scratch, out, stream);
   }
-  const size_t es = p.precision == 0 ? 16 : 8;
   const char* ib = static_cast<const char*>(in) + p.in.offset * (int64_t)es;
   char* ob = static_cast<char*>(out) + p.out.offset * (int64_t)es;
-  auto launch = [&](const GroupDesc& g, const void* a, void* b) -> cudaError_t {
+  auto launch = [&](int gi, const GroupDesc& g, const void* a, void* b) -> cudaError_t {
     if (p.precision == 0) return launch_group_f64(g, p.fwd, a, b, stream);
+    if (p.tile_stream && ((uintptr_t)a % 8) == 0 && ((uintptr_t)b % 8) == 0)
+      return launch_tile_stream_f32(g, p.fwd, a, b, p.ts_grid[gi], stream);
     return launch_group_f32(g, p.fwd, a, b, stream);
   };
   if (p.ngroups == 1) {
@@ -484,7 +531,7 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     if (p.stream && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)
       return launch_stream_f32(p.groups[0], p.fwd, ib, ob, p.howmany, p.stream_grid, p.d_status,
                                stream);
-    return launch(p.groups[0], ib, ob);
+    return launch(0, p.groups[0], ib, ob);
   }
   // two groups: the intermediate goes to `out` when it does not alias the input, else to the
   // plan's scratch buffer (allocated on first use)
@@ -516,9 +563,9 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
   g2.in_line = z_line;
   g2.in_sub = z_stride;
   g2.in_elem = P * z_stride;
-  cudaError_t e = launch(g1, ib, zb);
+  cudaError_t e = launch(0, g1, ib, zb);
   if (e != cudaSuccess) return e;
-  return launch(g2, zb, ob);
+  return launch(1, g2, zb, ob);
 }
 
 }  // namespace lfg

@@ -73,6 +73,7 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
   // radix sequences and twiddle tables of every class, in one device buffer
   std::vector<PassTables> tables(ncls);
   std::vector<size_t> base(ncls, 0);
+  std::vector<int> split_c(ncls, 0);
   size_t total = 0;
   r.flops = 0;
   for (int c = 0; c < ncls; ++c) {
@@ -82,6 +83,12 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
     std::string msg = check_radices(n, r.class_radices[c]);
     if (!msg.empty()) return "size " + std::to_string(n) + ": " + msg;
     tables[c] = make_pass_tables(n, r.fwd, r.class_radices[c], prec);
+    // pass grouping: the per-size strategy splits at the shared-memory limit, the persistent
+    // kernel at opt.single_max; the second group's tables are stored transposed
+    split_c[c] = split_point(n, r.class_radices[c],
+                             r.per_size_mode ? max_single_group(prec) : opt.single_max);
+    if (split_c[c] < 0) return "size " + std::to_string(n) + " needs more than two pass groups";
+    transpose_second_group(tables[c], r.class_radices[c], split_c[c], {});
     base[c] = total;
     total += tables[c].values.size();
     r.flops += plan_ops(n, r.class_radices[c]) * (double)r.class_count[c];
@@ -104,8 +111,7 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
     RaggedClass& rc = r.classes_host[c];
     rc.n = (int)n;
     const void* tw = static_cast<const char*>(r.d_twiddles) + base[c] * scal;
-    int split = split_point(n, rs, opt.single_max);
-    if (split < 0) return "size " + std::to_string(n) + " needs more than two pass groups";
+    const int split = split_c[c];
     const double ops_one = plan_ops(n, rs);
     if (split == (int)rs.size()) {
       rc.ngroups = 1;
@@ -204,7 +210,7 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
       PerSizeLaunch L;
       L.in_base = in_sorted[f + i];
       L.out_base = out_sorted[f + i];
-      int split = split_point(n, rs, max_single_group(prec));
+      const int split = split_c[c];
       if (split == (int)rs.size()) {
         L.ngroups = 1;
         GroupDesc& g = L.g[0];

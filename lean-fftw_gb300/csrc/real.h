@@ -1,4 +1,4 @@
-// Real-input / real-output transforms (see real_f64.cu).
+// Real-input / real-output transforms (kernels in real.cu).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -10,7 +10,7 @@ namespace lfg {
 
 // Lines of a real transform of even size N = 2M: line L = b * rows + r (b: vector index, r:
 // row of a rank-2 transform, rows = 1 for rank 1).  The real side of line L starts at double
-// r_off + b*r_bdist + r*r_rdist (even, so pairs load as 16-byte values) with unit stride;
+// r_off + b*r_bdist + r*r_rdist (even, so pairs load as one complex value) with unit stride;
 // the complex side (M+1 values) at complex element c_off + b*c_bdist + r*c_rdist.
 struct RealDesc {
   GroupDesc g;                 // the size-M passes, one group (nsub = 1, tile of g.C lines)
@@ -27,8 +27,9 @@ struct RealDesc {
   int adjoint;
 };
 
-cudaError_t prepare_real_kernels_f64();
-cudaError_t launch_real_f64(const RealDesc& d, bool r2c, const void* in, void* out,
-                            cudaStream_t stream);
+cudaError_t prepare_real_kernels();
+// precision 0: binary64 (double lines, double2 spectrum); 1: binary32 (float, float2)
+cudaError_t launch_real(const RealDesc& d, int precision, bool r2c, const void* in, void* out,
+                        cudaStream_t stream);
 
 }  // namespace lfg

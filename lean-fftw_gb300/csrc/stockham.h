@@ -15,7 +15,8 @@
 //     stride-N/P subsequence x[b + (N/P) i], written contiguously to z[b*P + m];
 //   * second group (passes T..s-1): sub-problem m < P is the stride-P subsequence
 //     z[q*P + m]; it is read and written in place, and the table index of a twiddle is
-//     k = k_local*P + m.
+//     k = k_local*P + m (the planner stores these tables transposed, at m*ns_local + k_local,
+//     so that a warp's threads, which walk k_local, read neighbouring entries).
 //
 // Both facts follow from the pass formula: after passes 0..T-1, positions b*P..b*P+P-1 hold
 // the size-P transform of x[b + (N/P) i]; every later pass maps positions = m (mod P) to
@@ -24,6 +25,12 @@
 // the reference transform for the same radix sequence.
 #pragma once
 #include <cstdint>
+
+#ifdef __CUDACC__
+#define LFG_HD __host__ __device__
+#else
+#define LFG_HD
+#endif
 
 namespace lfg {
 
@@ -54,6 +61,14 @@ inline int fastdiv_host(int n, FastDiv f) {
   return (int)((t + (uint32_t)n) >> f.l);
 }
 
+// Shared-memory tile layout: sub-problem c of a tile starts at c * sub_pitch(M), and its
+// element i sits at i + i/16 (one padding element after every 16).  The padding spreads a
+// pass's stride-R stores over the banks; the odd pitch puts neighbouring sub-problems in
+// different banks (tile copies of strided sub-problems and passes with fewer than 32
+// butterflies per sub-problem walk across sub-problems).
+LFG_HD constexpr int sub_pitch(int M) { return (M + (M >> 4)) | 1; }
+LFG_HD constexpr int64_t tile_elems(int64_t C, int M) { return C * (int64_t)sub_pitch(M); }
+
 struct PassDesc {
   int R;                 // radix of the pass
   int ns_loc;            // product of the group's earlier radices
@@ -76,7 +91,7 @@ struct GroupDesc {
   int64_t total_sub;     // lines * nsub
   int64_t in_line, in_sub, in_elem;
   int64_t out_line, out_sub, out_elem;
-  int kmul;              // table index k = k_loc * kmul + (twsub ? s % nsub : 0)
+  int kmul;              // product of the radices before the group (P for a second group)
   int twsub;
   double scale;          // outputs multiplied by this on store unless it is exactly 1
   FastDiv fd_m, fd_c, fd_nsub;   // divisors M, C, nsub (set_divisors)

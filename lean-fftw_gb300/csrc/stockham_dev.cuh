@@ -42,11 +42,11 @@ struct Prec<float> {
 };
 
 
-// Shared-memory tiles are padded by one element after every 16: a Stockham pass stores its
+// Within a sub-problem, one padding element after every 16: a Stockham pass stores its
 // outputs at stride R (up to 16 elements = 128 or 256 bytes) between neighbouring threads,
 // which would put a whole warp on one bank; with the padding the stride is 17 elements.
+// Sub-problems start sub_pitch(M) elements apart (stockham.h).
 __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
-__host__ __device__ constexpr int padded_elems(int n) { return n + (n >> 4) + 1; }
 
 // n / d for 0 <= n < 2^31 with the plan's FastDiv of d (stockham.h).
 __device__ __forceinline__ int fdiv(int n, const FastDiv& f) {
@@ -72,29 +72,30 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
   const T* __restrict__ tw = static_cast<const T*>(pd.tw);
   const int64_t nsg = pd.ns_g;
   const FastDiv fd_mr = pd.fd_mr, fd_ns = pd.fd_ns;
+  const int PM = sub_pitch(M);
   for (int q = threadIdx.x; q < nb; q += blockDim.x) {
     const int c = fdiv(q, fd_mr);
     const int j = q - c * MR;
     T x[TW ? 4 * R - 2 : 2 * R];
     T y[2 * R];
-    const int s0i = c * M + j;
+    const Cx* sc = src + (SRCPAD ? c * PM : c * M);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const int si = s0i + r * MR;
-      const Cx v = src[SRCPAD ? spad(si) : si];
+      const int si = j + r * MR;
+      const Cx v = sc[SRCPAD ? spad(si) : si];
       x[2 * r] = v.x;
       x[2 * r + 1] = v.y;
     }
     const int b = fdiv(j, fd_ns);
     const int k = j - b * ns;
-    // table index of the twiddle: k_loc * kmul + sub-problem index within the line (second
-    // group only; tiles may straddle lines, so the index wraps at nsub)
-    int msub = 0;
+    // table index of the twiddle: k (one group, or the first), or, in the second group,
+    // m * ns_loc + k with m the sub-problem index within its line (the planner stores those
+    // tables transposed; tiles may straddle lines, so m wraps at nsub)
+    int64_t kg = k;
     if (sub0 >= 0) {
       const int t = sub0 + c;
-      msub = t - fdiv(t, fd_nsub) * nsub;
+      kg = (int64_t)(t - fdiv(t, fd_nsub) * nsub) * ns + k;
     }
-    const int64_t kg = (int64_t)k * kmul + msub;
     if (MODE == 1) {
 #pragma unroll
       for (int r = 0; r < R - 1; ++r) {
@@ -116,9 +117,10 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
       }
     }
     P::template Bfly<FWD, R, TW>::run(x, y);
-    const int d0 = c * M + b * ns * R + k;
+    const int d0 = b * ns * R + k;
+    Cx* dc = dst + c * PM;
 #pragma unroll
-    for (int r = 0; r < R; ++r) dst[spad(d0 + r * ns)] = P::mk(y[2 * r], y[2 * r + 1]);
+    for (int r = 0; r < R; ++r) dc[spad(d0 + r * ns)] = P::mk(y[2 * r], y[2 * r + 1]);
   }
 }
 
@@ -190,9 +192,12 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
   if (elem_fast && nsub == 1 && lines.pitch(LOAD) == M && g.scale == 1.0) {
     // back-to-back lines: the tile is one contiguous range of global memory
     const int64_t base = (LOAD ? lines.in(s0) : lines.out(s0));
+    const int PM = sub_pitch(M);
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
-      if (LOAD) tile[spad(idx)] = gin[base + idx];
-      else gout[base + idx] = tile[spad(idx)];
+      const int c = fdiv(idx, g.fd_m);
+      const int t = c * PM + spad(idx - c * M);
+      if (LOAD) tile[t] = gin[base + idx];
+      else gout[base + idx] = tile[t];
     }
     return;
   }
@@ -202,6 +207,9 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
   // strided sub-problems: neighbouring threads take neighbouring sub-problems, over the full
   // tile width g.C (a partial last tile skips the missing columns)
   const int nn = elem_fast ? n : g.C * M;
+  const bool unit = g.scale == 1.0;
+  const T sc = (T)g.scale;
+  const int PM = sub_pitch(M);
   for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
     int c, i;
     if (elem_fast) {
@@ -218,12 +226,11 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
     const int64_t sub = t - ql * nsub;
     const int64_t a = (LOAD ? lines.in(line) : lines.out(line)) + sub * sub_st + (int64_t)i * elem_st;
     if (LOAD) {
-      tile[spad(c * M + i)] = gin[a];
-    } else if (g.scale == 1.0) {
-      gout[a] = tile[spad(c * M + i)];
+      tile[c * PM + spad(i)] = gin[a];
+    } else if (unit) {
+      gout[a] = tile[c * PM + spad(i)];
     } else {
-      const auto v = tile[spad(c * M + i)];
-      const T sc = (T)g.scale;
+      const auto v = tile[c * PM + spad(i)];
       gout[a] = P::mk(P::mul(v.x, sc), P::mul(v.y, sc));
     }
   }
@@ -255,7 +262,7 @@ __device__ __forceinline__ void process_tile(const GroupDesc& g, const Lines& li
                                              int C, const typename Prec<T>::C* in,
                                              typename Prec<T>::C* out, typename Prec<T>::C* smem) {
   auto* A = smem;
-  auto* B = smem + padded_elems(g.C * g.M);
+  auto* B = smem + tile_elems(g.C, g.M);
   copy_tile<T, true>(A, in, nullptr, g, lines, s0, C);
   __syncthreads();
   // second group: the sub-problem index within the line enters the twiddle index

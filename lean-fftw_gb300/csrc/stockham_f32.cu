@@ -10,6 +10,8 @@
 // arithmetic.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "stockham_dev.cuh"
 
 namespace lfg {
@@ -82,9 +84,9 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
                   int64_t lines, int* status) {
   extern __shared__ __align__(128) float2 smem_f32s[];
   __shared__ __align__(8) uint64_t bars[kStages];
-  const int M = g.M, CM = g.C * g.M;
+  const int M = g.M, CM = g.C * g.M, PM = sub_pitch(g.M);
   float2* A = smem_f32s + kStages * CM;       // stage buffers unpadded (bulk-copy targets)
-  float2* B = A + padded_elems(CM);
+  float2* B = A + tile_elems(g.C, M);
   const int64_t ntiles = (lines + g.C - 1) / g.C;
   bool pending[kStages];
   if (threadIdx.x == 0) {
@@ -142,7 +144,9 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
     const int n4 = C * M / 2;
     const float sc = (float)g.scale;
     for (int i = threadIdx.x; i < n4; i += blockDim.x) {
-      const float2 a = src[spad(2 * i)], b = src[spad(2 * i + 1)];
+      const int e = 2 * i, c = fdiv(e, g.fd_m), ii = e - c * M;   // M even: ii + 1 < M
+      const float2* row = src + c * PM;
+      const float2 a = row[spad(ii)], b = row[spad(ii + 1)];
       if (g.scale == 1.0) o4[i] = make_float4(a.x, a.y, b.x, b.y);
       else o4[i] = make_float4(__fmul_rn(a.x, sc), __fmul_rn(a.y, sc), __fmul_rn(b.x, sc), __fmul_rn(b.y, sc));
     }
@@ -155,6 +159,85 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
     for (int k = 0; k < kStages; ++k)
       if (pending[k]) mbar_wait(&bars[k], (parity >> k) & 1);
   }
+}
+
+// ---- asynchronous element copies (cp.async) for strided tiles ------------------------------
+
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Issue the copies of tile `s0` (C of g.C sub-problems) into the padded tile buffer S; same
+// element order and addressing as the synchronous tile load (stockham_dev.cuh: copy_tile).
+__device__ __forceinline__ void load_tile_async(float2* S, const float2* in, const GroupDesc& g,
+                                                int64_t s0, int C) {
+  const int M = g.M, nsub = g.nsub, PM = sub_pitch(M);
+  const int64_t line0 = s0 / nsub;
+  const int sub0 = (int)(s0 - line0 * nsub);
+  const bool elem_fast = g.in_elem == 1;
+  const int nn = elem_fast ? C * M : g.C * M;
+#pragma unroll 4
+  for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
+    int c, i;
+    if (elem_fast) {
+      c = fdiv(idx, g.fd_m);
+      i = idx - c * M;
+    } else {
+      i = fdiv(idx, g.fd_c);
+      c = idx - i * g.C;
+      if (c >= C) continue;
+    }
+    const int t = sub0 + c;
+    const int ql = fdiv(t, g.fd_nsub);
+    const int64_t a = (line0 + ql) * g.in_line + (int64_t)(t - ql * nsub) * g.in_sub +
+                      (int64_t)i * g.in_elem;
+    cp_async8(S + c * PM + spad(i), in + a);
+  }
+  cp_async_commit();
+}
+
+// Persistent binary32 kernel for tiles of strided sub-problems (the groups of two-group plans
+// and strided batches): each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...;
+// the next tile's elements are copied asynchronously into a stage buffer while the CTA runs
+// the later passes of the current tile and stores it, so HBM reads overlap the arithmetic
+// and the stores.  Waits are cp.async group waits (no polling).
+template <bool FWD>
+__global__ void __launch_bounds__(kGroupThreads)
+tile_stream_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
+  extern __shared__ __align__(16) float2 smem_ts[];
+  const int PE = (int)tile_elems(g.C, g.M);
+  float2* S = smem_ts;
+  float2* A = S + PE;
+  float2* B = A + PE;
+  const int64_t ntiles = (g.total_sub + g.C - 1) / g.C;
+  const StridedLines lines{g.in_line, g.out_line};
+  auto count = [&](int64_t tile) { return (int)min((int64_t)g.C, g.total_sub - tile * g.C); };
+  if ((int64_t)blockIdx.x < ntiles) load_tile_async(S, in, g, (int64_t)blockIdx.x * g.C, count(blockIdx.x));
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t s0 = tile * g.C;
+    const int C = count(tile);
+    cp_async_wait_all();
+    __syncthreads();
+    const int sub0 = g.twsub ? (int)(s0 % g.nsub) : -1;
+    run_pass_t<float, FWD>(S, A, C, g.M, g.pass[0], g.kmul, sub0, g.nsub, g.fd_nsub);
+    __syncthreads();
+    // the stage buffer has been consumed: start copying this CTA's next tile
+    const int64_t next = tile + gridDim.x;
+    if (next < ntiles) load_tile_async(S, in, g, next * g.C, count(next));
+    float2* src = A;
+    float2* dst = B;
+    for (int t = 1; t < g.npass; ++t) {
+      run_pass_t<float, FWD>(src, dst, C, g.M, g.pass[t], g.kmul, sub0, g.nsub, g.fd_nsub);
+      __syncthreads();
+      float2* tmp = src;
+      src = dst;
+      dst = tmp;
+    }
+    copy_tile<float, false>(src, nullptr, out, g, lines, s0, C);
+  }
+  cp_async_wait_all();
 }
 
 template <class K>
@@ -173,11 +256,38 @@ cudaError_t prepare_group_kernels_f32() {
   if (e != cudaSuccess) return e;
   if ((e = allow_max_smem(group_kernel_f32<false>)) != cudaSuccess) return e;
   if ((e = allow_max_smem(stream_kernel_f32<true>)) != cudaSuccess) return e;
-  return allow_max_smem(stream_kernel_f32<false>);
+  if ((e = allow_max_smem(stream_kernel_f32<false>)) != cudaSuccess) return e;
+  if ((e = allow_max_smem(tile_stream_kernel_f32<true>)) != cudaSuccess) return e;
+  return allow_max_smem(tile_stream_kernel_f32<false>);
+}
+
+size_t tile_stream_smem_bytes_f32(const GroupDesc& g) {
+  return 3 * (size_t)tile_elems(g.C, g.M) * sizeof(float2);
+}
+
+int tile_stream_blocks_per_sm_f32(const GroupDesc& g) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tile_stream_kernel_f32<true>, kGroupThreads,
+                                                    tile_stream_smem_bytes_f32(g)) != cudaSuccess)
+    return 1;
+  return nb > 0 ? nb : 1;
+}
+
+cudaError_t launch_tile_stream_f32(const GroupDesc& gd, bool fwd, const void* in, void* out,
+                                   unsigned grid, cudaStream_t stream) {
+  GroupDesc g = gd;
+  set_divisors(g);
+  const int64_t ntiles = (g.total_sub + g.C - 1) / g.C;
+  if (ntiles <= 0) return cudaSuccess;
+  const unsigned gr = (unsigned)std::min<int64_t>(grid, ntiles);
+  auto kern = fwd ? tile_stream_kernel_f32<true> : tile_stream_kernel_f32<false>;
+  kern<<<gr, kGroupThreads, tile_stream_smem_bytes_f32(g), stream>>>(
+      g, static_cast<const float2*>(in), static_cast<float2*>(out));
+  return cudaGetLastError();
 }
 
 size_t stream_smem_bytes_f32(const GroupDesc& g) {
-  return ((size_t)kStages * g.C * g.M + 2 * (size_t)padded_elems(g.C * g.M)) * sizeof(float2);
+  return ((size_t)kStages * g.C * g.M + 2 * (size_t)tile_elems(g.C, g.M)) * sizeof(float2);
 }
 
 int stream_blocks_per_sm_f32(const GroupDesc& g) {
@@ -203,7 +313,7 @@ cudaError_t launch_group_f32(const GroupDesc& gd, bool fwd, const void* in, void
                              cudaStream_t stream) {
   GroupDesc g = gd;
   set_divisors(g);
-  const size_t smem = 2 * (size_t)padded_elems(g.C * g.M) * sizeof(float2);
+  const size_t smem = 2 * (size_t)tile_elems(g.C, g.M) * sizeof(float2);
   const int64_t grid = (g.total_sub + g.C - 1) / g.C;
   if (grid <= 0) return cudaSuccess;
   auto kern = fwd ? group_kernel_f32<true> : group_kernel_f32<false>;

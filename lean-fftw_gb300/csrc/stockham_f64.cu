@@ -100,7 +100,7 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
 }  // namespace
 
 size_t group_smem_bytes_f64(const GroupDesc& g) {
-  return 2 * (size_t)padded_elems(g.C * g.M) * sizeof(double2);
+  return 2 * (size_t)tile_elems(g.C, g.M) * sizeof(double2);
 }
 
 size_t ragged_smem_bytes_f64(const RaggedClass& c) {

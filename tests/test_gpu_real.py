@@ -112,3 +112,53 @@ def test_rdft2_spec_vector():
         got = o[1 + b * cpitch: 1 + b * cpitch + n // 2 + 1]
         e = O.rel_l2(got, O.dd_r2c(x[None, :]))
         assert e < 3e-16, e
+
+
+# ---- binary32 variant -------------------------------------------------------------------
+U32 = 2.0 ** -24
+
+
+@pytest.mark.parametrize("n", [2, 6, 16, 60, 512, 1024, 8192, 10368])
+def test_fp32_r2c_c2r_error(n):
+    """Binary32 r2c and c2r (twiddles rounded once from the binary64 tables): relative L2
+    error against the double-double DFT of the same binary32 data at the binary32 level."""
+    B = 4
+    rng = np.random.default_rng(n + 100)
+    x = (rng.random((B, n)) - 0.5).astype(np.float32)
+    plan = lfg.plan_r2c(n, B, precision="f32")
+    out = torch.empty((B, n // 2 + 1), dtype=torch.complex64, device="cuda")
+    plan.execute(torch.from_numpy(x).cuda(), out)
+    torch.cuda.synchronize()
+    X = out.cpu().numpy().astype(np.complex128)
+    bound = 4 * U32 * max(1.0, np.sqrt(np.log2(n)))
+    e = O.rel_l2(X, O.dd_r2c(x.astype(np.float64), nthreads=8))
+    assert e < bound, (n, e)
+    h = X.astype(np.complex64)
+    back = lfg.plan_c2r(n, B, precision="f32")
+    y = torch.empty((B, n), dtype=torch.float32, device="cuda")
+    back.execute(torch.from_numpy(h).cuda(), y)
+    torch.cuda.synchronize()
+    e2 = O.rel_l2(y.cpu().numpy().astype(np.float64),
+                  O.dd_c2r(h.astype(np.complex128), n, nthreads=8))
+    assert e2 < bound, (n, e2)
+
+
+def test_fp32_rank2_64x512x512():
+    """The large-image configuration: 64 images of 512 x 512, binary32 r2c and c2r."""
+    n0 = n1 = 512
+    B = 64
+    x = (np.random.default_rng(5).random((B, n0, n1)) - 0.5).astype(np.float32)
+    plan = lfg.plan_r2c_2d(n0, n1, B, precision="f32")
+    out = torch.empty((B, n0, n1 // 2 + 1), dtype=torch.complex64, device="cuda")
+    plan.execute(torch.from_numpy(x).cuda(), out)
+    torch.cuda.synchronize()
+    X = out.cpu().numpy()
+    ref = np.fft.rfft2(x[:2].astype(np.float64))           # two images checked in full
+    e = np.linalg.norm(X[:2] - ref) / np.linalg.norm(ref)
+    assert e < 8 * U32, e
+    back = lfg.plan_c2r_2d(n0, n1, B, precision="f32")
+    y = torch.empty((B, n0, n1), dtype=torch.float32, device="cuda")
+    back.execute(out, y)
+    torch.cuda.synchronize()
+    r = y.cpu().numpy() / (n0 * n1)
+    assert np.max(np.abs(r - x)) < 64 * U32, np.max(np.abs(r - x))
