@@ -45,7 +45,9 @@ typedef struct lfg_plan lfg_plan;
  * FFI.lean:32-47): doubles holding small integers
  *   [kind, sign, rank, vrank, inRe, inIm, outRe, outIm,
  *    (n, is, os) x rank, (n, is, os) x vrank, r2rkind x rank]
- * kind 0 = complex DFT, 1 = rdft2 (r2c when sign < 0, c2r otherwise); strides and offsets
+ * kind 0 = complex DFT (any rank and vector rank), 1 = rdft2 (r2c when sign < 0, c2r
+ * otherwise; rank 1-2, vector rank <= 1), 2 = r2r (any rank, one kind per dimension, see
+ * lfg_plan_r2r); strides and offsets
  * are in real scalars of the plan's precision (doubles for LFG_F64, as in the reference;
  * floats for LFG_F32), relative to the pointers later given to lfg_execute.  Replaces
  * `lfftw_generic_plan` (LeanFFTW/FFI.lean:50-52) for the kinds and layouts this library
@@ -82,6 +84,16 @@ lfg_status lfg_plan_r2c_2d(size_t n0, size_t n1, size_t howmany, lfg_precision p
                            unsigned flags, lfg_plan **out);
 lfg_status lfg_plan_c2r_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
                            unsigned flags, lfg_plan **out);
+
+/* Real-to-real transforms of one of libbench2's eleven kinds (numbering as lean-fftw's FFI,
+ * LeanFFTW/FFI.lean:29-31): 0 R2HC, 1 HC2R, 2 DHT, 3 REDFT00, 4 REDFT01, 5 REDFT10,
+ * 6 REDFT11, 7 RODFT00, 8 RODFT01, 9 RODFT10, 10 RODFT11; `howmany` contiguous lines of n
+ * real scalars.  Computed as lean-fftw's generic engine defines them: an exact symmetric
+ * embedding into a complex DFT of size 1, 2, 4 or 8 times n (`R2RKind.embed/extract`,
+ * LeanFFTW/Core/Problem.lean:64-112), which must be 13-smooth.  Multi-dimensional r2r
+ * problems (one kind per dimension) go through lfg_plan_spec with kind 2. */
+lfg_status lfg_plan_r2r(size_t n, int kind, size_t howmany, lfg_precision precision,
+                        unsigned flags, lfg_plan **out);
 
 /* With LFG_ADJOINT, lfg_plan_r2c doubles its output bins 1..n/2-1 (the gradient of c2r) and
  * lfg_plan_c2r halves its input bins 1..n/2-1 (the gradient of r2c), both exactly, inside

@@ -85,18 +85,32 @@ int64_t span_scalars(const lfg::Side& s, int64_t n, int64_t howmany, int64_t per
   return (s.offset + (n - 1) * s.stride + (howmany - 1) * s.dist + 1) * per_elem;
 }
 
-lfg_status finish_c2c(lfg::Plan& p, lfg_plan** out) {
+// Device part of a 1-D complex plan: kernels set up, autotuning, groups and tables.
+lfg_status build_c2c_device(lfg::Plan& p) {
   // binary64 is bound by the FP64 pipe: two groups of small tiles (more CTAs per SM) beat one
   // group with a CTA-sized tile above 2048 points; binary32 is bound by HBM: as few groups as fit
+  const bool user_split = p.single_max > 0 || p.tile > 0;
   if (p.single_max == 0 && p.precision == 0) p.single_max = single_max_default();
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   p.device = dev;
+  // a small batch leaves most SMs idle with one CTA per tile of whole transforms, and one
+  // SM's FP64 pipe needs ~8 us for a 1024-point transform: split the transform into two
+  // balanced pass groups of one sub-problem per CTA instead, so that it spreads over
+  // N/P + P CTAs (lower latency; same operations, same result bits)
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t c1 = std::max<int64_t>(1, tile_target() / std::max<int64_t>(p.n, 1));
+  const int64_t tiles1 = (p.howmany * p.howmany2 + c1 - 1) / c1;
+  if (!user_split && !p.measure && p.n >= 256 && 4 * tiles1 < sms) {
+    p.single_max = p.n - 1;     // forces the most balanced two-group split
+    p.tile = 1;                 // one sub-problem per CTA
+  }
   if (!p.empty) {
     e = p.precision == 0 ? lfg::prepare_group_kernels_f64() : lfg::prepare_group_kernels_f32();
     if (e != cudaSuccess) return cuda_fail(e, "kernel set-up");
-    if (p.measure) {
+    if (p.measure && p.howmany2 == 1) {
       std::string msg = lfg::tune_c2c(p, tile_target());
       if (!msg.empty()) return fail(LFG_ERR_CUDA, msg);
     }
@@ -106,6 +120,12 @@ lfg_status finish_c2c(lfg::Plan& p, lfg_plan** out) {
       return fail(LFG_ERR_UNSUPPORTED, msg);
     }
   }
+  return LFG_OK;
+}
+
+lfg_status finish_c2c(lfg::Plan& p, lfg_plan** out) {
+  lfg_status s = build_c2c_device(p);
+  if (s != LFG_OK) return s;
   p.in_span = span_scalars(p.in, p.n, p.howmany, 2);
   p.out_span = span_scalars(p.out, p.n, p.howmany, 2);
   lfg_plan* h = new (std::nothrow) lfg_plan;
@@ -205,6 +225,192 @@ lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision prec
   return finish_c2c(p, out);
 }
 
+// A dimension of the FFI spec in complex elements.
+struct CDim {
+  int64_t n, is, os;
+};
+
+// One r2r axis stage: lines of n real elements (`is`/`os` apart) in a batch of inner x outer
+// lines; the embedding of each line goes through a complex DFT of the embedding size.
+lfg_status build_r2r_child(lfg::Plan& c, int rkind, int64_t n, int64_t is, int64_t os,
+                           const CDim& inner, const CDim& outer, lfg_precision precision,
+                           unsigned flags) {
+  const int64_t M = lfg::r2r_embed_size(rkind, n);
+  if (M == 0) return fail(LFG_ERR_UNSUPPORTED, "r2r kind or size not defined (REDFT00 needs n >= 2)");
+  if (M > 1 && (M > ((int64_t)1 << 24) || !smooth13(M)))
+    return fail(LFG_ERR_UNSUPPORTED, "r2r embedding size " + std::to_string(M) +
+                                         " must be 13-smooth and at most 2^24");
+  const int64_t lines = inner.n * outer.n;
+  if (lines * M >= ((int64_t)1 << 31) || lines * n >= ((int64_t)1 << 31))
+    return fail(LFG_ERR_UNSUPPORTED, "r2r batch too large (2^31 embedded elements per plan)");
+  c.kind = lfg::Kind::R2R;
+  c.precision = precision;
+  c.fwd = rkind != lfg::kHC2R;
+  c.n = n;
+  c.howmany = lines;
+  lfg::R2RDesc& d = c.r2r;
+  d.kind = rkind;
+  d.n = n;
+  d.M = M;
+  d.lines = lines;
+  d.nl1 = std::max<int64_t>(1, inner.n);
+  d.in_off = d.out_off = 0;
+  d.in_stride = is;
+  d.out_stride = os;
+  d.in_dist = inner.is;
+  d.out_dist = inner.os;
+  d.in_dist2 = outer.is;
+  d.out_dist2 = outer.os;
+  d.fd_m = lfg::make_fastdiv((int)M);
+  d.fd_n = lfg::make_fastdiv((int)n);
+  d.fd_nl1 = lfg::make_fastdiv((int)d.nl1);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  c.device = dev;
+  const size_t ces = precision == 0 ? 16 : 8;
+  cudaError_t e = cudaMalloc(&c.d_r2r_buf, 2 * (size_t)lines * (size_t)M * ces);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc of the r2r buffers");
+  if (M > 1) {
+    auto dft = std::make_shared<lfg::Plan>();
+    dft->kind = lfg::Kind::C2C;
+    dft->precision = precision;
+    dft->fwd = c.fwd;
+    dft->n = M;
+    dft->howmany = lines;
+    dft->in = dft->out = {0, 1, M};
+    dft->no_comp = (flags & LFG_NO_COMPENSATION) != 0;
+    dft->radices = lfg::choose_radices(M, precision);
+    lfg_status s = build_c2c_device(*dft);
+    if (s != LFG_OK) return s;
+    c.flops = dft->flops;
+    c.r2r_dft = dft;
+  }
+  return LFG_OK;
+}
+
+// Multi-axis transforms, separable along each axis (lean-fftw's generic engine applies a
+// line operation along each axis over all other indices: `alongAxis`,
+// LeanFFTW/Core/Problem.lean:170-212).  Complex problems (rank >= 2, or vector rank >= 2) and
+// all r2r problems become one stage per axis, last axis first (complex axes of size 1 are
+// skipped), each an ordinary 1-D plan whose batch is every other dimension: dimensions that
+// nest (outer stride = inner count x inner stride on both sides) are merged, the two
+// innermost remaining ones are covered by one launch (lines, and blocks of lines), any
+// further ones by a host loop of launches.  The first stage reads the input; the later
+// stages work in place on the output.  Units: complex elements (c2c) or real scalars (r2r).
+lfg_status plan_separable(bool r2r, const std::vector<CDim>& T, const std::vector<CDim>& V,
+                          const std::vector<int>& kinds, int64_t in_off, int64_t out_off,
+                          int sign, lfg_precision precision, unsigned flags, lfg_plan** out) {
+  lfg::Plan p;
+  p.kind = r2r ? lfg::Kind::R2R : lfg::Kind::C2C;
+  p.precision = precision;
+  p.fwd = sign < 0;
+  p.n = 1;
+  p.howmany = 1;
+  for (const CDim& d : T) p.n *= d.n;
+  for (const CDim& d : V) p.howmany *= d.n;
+  p.empty = p.howmany == 0;
+  p.in.offset = in_off;
+  p.out.offset = out_off;
+  int64_t ihi = in_off, ohi = out_off;
+  for (const auto* L : {&T, &V})
+    for (const CDim& d : *L)
+      if (d.n > 1) {
+        ihi += (d.n - 1) * d.is;
+        ohi += (d.n - 1) * d.os;
+      }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  p.device = dev;
+  if (!p.empty) {
+    std::vector<int> axes;
+    for (int d = (int)T.size() - 1; d >= 0; --d)
+      if (T[d].n > 1 || r2r) axes.push_back(d);
+    if (axes.empty()) return fail(LFG_ERR_UNSUPPORTED, "all transform dimensions are 1 (a copy)");
+    for (size_t k = 0; k < axes.size(); ++k) {
+      const int d = axes[k];
+      const bool first = k == 0;
+      auto is_of = [&](const CDim& x) { return first ? x.is : x.os; };
+      std::vector<CDim> batch;
+      for (int e = 0; e < (int)T.size(); ++e)
+        if (e != d && T[e].n > 1) batch.push_back({T[e].n, is_of(T[e]), T[e].os});
+      for (const CDim& v : V)
+        if (v.n > 1) batch.push_back({v.n, is_of(v), v.os});
+      std::sort(batch.begin(), batch.end(), [](const CDim& a, const CDim& b) {
+        return a.os != b.os ? a.os < b.os : a.is < b.is;
+      });
+      for (size_t i = 0; i + 1 < batch.size();) {
+        CDim& a = batch[i];
+        const CDim& b = batch[i + 1];
+        if (b.is == a.n * a.is && b.os == a.n * a.os) {
+          a.n *= b.n;
+          batch.erase(batch.begin() + i + 1);
+        } else {
+          ++i;
+        }
+      }
+      const CDim inner = batch.size() > 0 ? batch[0] : CDim{1, 0, 0};
+      const CDim outer = batch.size() > 1 ? batch[1] : CDim{1, 0, 0};
+      lfg::AxisStage stage;
+      int64_t nl = 1;
+      for (size_t i = 2; i < batch.size(); ++i) nl *= batch[i].n;
+      if (nl > (1 << 16)) {
+        lfg::free_plan_memory(p);
+        return fail(LFG_ERR_UNSUPPORTED, "too many launches for this dimension nesting");
+      }
+      for (int64_t q = 0; q < nl; ++q) {
+        int64_t r = q, oi = first ? in_off : out_off, oo = out_off;
+        for (size_t i = 2; i < batch.size(); ++i) {
+          oi += (r % batch[i].n) * batch[i].is;
+          oo += (r % batch[i].n) * batch[i].os;
+          r /= batch[i].n;
+        }
+        stage.loops.push_back({oi, oo});
+      }
+      auto st = std::make_shared<lfg::Plan>();
+      lfg::Plan& c = *st;
+      lfg_status s;
+      if (r2r) {
+        s = build_r2r_child(c, kinds[d], T[d].n, is_of(T[d]), T[d].os, inner, outer, precision, flags);
+      } else {
+        c.kind = lfg::Kind::C2C;
+        c.precision = precision;
+        c.fwd = p.fwd;
+        c.n = T[d].n;
+        c.in = {0, is_of(T[d]), inner.is};
+        c.out = {0, T[d].os, inner.os};
+        c.howmany = inner.n;
+        c.howmany2 = outer.n;
+        c.in_dist2 = outer.is;
+        c.out_dist2 = outer.os;
+        c.no_comp = (flags & LFG_NO_COMPENSATION) != 0;
+        c.radices = lfg::choose_radices(c.n, precision);
+        s = build_c2c_device(c);
+      }
+      if (s != LFG_OK) {
+        lfg::free_plan_memory(c);
+        lfg::free_plan_memory(p);
+        return s;
+      }
+      p.flops += c.flops * (double)nl;
+      const std::vector<int>& rs = r2r && c.r2r_dft ? c.r2r_dft->radices : c.radices;
+      p.radices.insert(p.radices.end(), rs.begin(), rs.end());
+      stage.plan = st;
+      p.stages.push_back(std::move(stage));
+    }
+  }
+  const int64_t per = r2r ? 1 : 2;
+  p.in_span = per * (ihi + 1);
+  p.out_span = per * (ohi + 1);
+  lfg_plan* h = new (std::nothrow) lfg_plan;
+  if (!h) {
+    lfg::free_plan_memory(p);
+    return fail(LFG_ERR_NOMEM, "host allocation");
+  }
+  h->p = p;
+  *out = h;
+  return LFG_OK;
+}
+
 }  // namespace
 
 void lfg::set_last_error(const std::string& msg) { g_last_error = msg; }
@@ -234,6 +440,17 @@ lfg_status lfg_plan_r2c_2d(size_t n0, size_t n1, size_t howmany, lfg_precision p
 lfg_status lfg_plan_c2r_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
                            unsigned flags, lfg_plan** out) {
   return plan_real_common(false, n0, n1, howmany, precision, flags, out);
+}
+
+lfg_status lfg_plan_r2r(size_t n, int kind, size_t howmany, lfg_precision precision,
+                        unsigned flags, lfg_plan** out) {
+  if (!out) return fail(LFG_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (precision != LFG_F64 && precision != LFG_F32) return fail(LFG_ERR_INVALID, "bad precision");
+  if (kind < 0 || kind > 10) return fail(LFG_ERR_INVALID, "r2r kind outside 0..10");
+  if (n < 1) return fail(LFG_ERR_INVALID, "size must be >= 1");
+  const std::vector<CDim> T{{(int64_t)n, 1, 1}}, V{{(int64_t)howmany, (int64_t)n, (int64_t)n}};
+  return plan_separable(true, T, V, {kind}, 0, 0, -1, precision, flags, out);
 }
 
 lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision precision,
@@ -313,17 +530,52 @@ lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precisi
     if (p.empty) L.howmany = 1;
     return finish_real(p, L, out);
   }
-  if (kind != 0) return fail(LFG_ERR_UNSUPPORTED, "r2r (kind 2) is not executed on the GPU");
+  if (kind == 2) {
+    // r2r (Core/Problem.lean:237-250): real data, one kind per transform dimension
+    if (nspec < (size_t)(8 + 3 * (rank + vrank) + rank))
+      return fail(LFG_ERR_INVALID, "r2r spec lacks the kinds");
+    if (rank < 1) return fail(LFG_ERR_UNSUPPORTED, "rank-0 problems (copies) are not executed");
+    std::vector<CDim> T, V;
+    std::vector<int> kinds;
+    for (int64_t i = 0; i < rank + vrank; ++i) {
+      int64_t n, is, os;
+      dim(i, &n, &is, &os);
+      if (n < 0 || (i < rank && n < 1)) return fail(LFG_ERR_INVALID, "bad dimension");
+      if (n > 1 && (is <= 0 || os <= 0)) return fail(LFG_ERR_UNSUPPORTED, "strides must be positive");
+      (i < rank ? T : V).push_back(CDim{n, is, os});
+    }
+    for (int64_t d = 0; d < rank; ++d) {
+      const int k = (int)spec[8 + 3 * (rank + vrank) + d];
+      if (k < 0 || k > 10) return fail(LFG_ERR_INVALID, "r2r kind outside 0..10");
+      kinds.push_back(k);
+    }
+    if (inRe < 0 || outRe < 0) return fail(LFG_ERR_UNSUPPORTED, "negative offsets");
+    return plan_separable(true, T, V, kinds, inRe, outRe, sign, precision, flags, out);
+  }
+  if (kind != 0) return fail(LFG_ERR_INVALID, "kind must be 0, 1 or 2");
   for (int64_t d = 0; d < rank; ++d) {
     int64_t n, is, os;
     dim(d, &n, &is, &os);
     if (n < 1) return fail(LFG_ERR_UNSUPPORTED, "transform dimension must be >= 1");
   }
-  if (rank != 1) return fail(LFG_ERR_UNSUPPORTED, "only rank-1 transforms are executed so far");
-  if (vrank > 1) return fail(LFG_ERR_UNSUPPORTED, "vector rank > 1 not executed so far");
+  if (rank < 1) return fail(LFG_ERR_UNSUPPORTED, "rank-0 problems (copies) are not executed");
   // interleaved complex data: imaginary part one double after the real part, even strides
   if (inIm != inRe + 1 || outIm != outRe + 1 || inRe < 0 || outRe < 0 || (inRe & 1) || (outRe & 1))
     return fail(LFG_ERR_UNSUPPORTED, "only interleaved, complex-aligned layouts are executed");
+  if (rank > 1 || vrank > 1) {
+    std::vector<CDim> T, V;
+    for (int64_t i = 0; i < rank + vrank; ++i) {
+      int64_t n, is, os;
+      dim(i, &n, &is, &os);
+      if (n < 0) return fail(LFG_ERR_INVALID, "negative dimension");
+      if (n > 1 && ((is & 1) || (os & 1) || is <= 0 || os <= 0))
+        return fail(LFG_ERR_UNSUPPORTED, "strides must be positive multiples of a complex element");
+      if (i < rank && (n > ((int64_t)1 << 24) || (n > 1 && !smooth13(n))))
+        return fail(LFG_ERR_UNSUPPORTED, "transform sizes must be 13-smooth and at most 2^24");
+      (i < rank ? T : V).push_back(CDim{n, is / 2, os / 2});
+    }
+    return plan_separable(false, T, V, {}, inRe / 2, outRe / 2, sign, precision, flags, out);
+  }
   int64_t n, is, os;
   dim(0, &n, &is, &os);
   int64_t vn = 1, vis = 0, vos = 0;
@@ -407,7 +659,12 @@ lfg_status lfg_set_scale(lfg_plan* plan, double scale) {
   if (!std::isfinite(scale)) return fail(LFG_ERR_INVALID, "scale must be finite");
   lfg::Plan& p = plan->p;
   if (p.kind != lfg::Kind::C2C) return fail(LFG_ERR_UNSUPPORTED, "scaling applies to complex plans");
-  if (p.ngroups >= 1) p.groups[p.ngroups - 1].scale = scale;
+  if (!p.stages.empty()) {
+    lfg::Plan& last = *p.stages.back().plan;
+    if (last.ngroups >= 1) last.groups[last.ngroups - 1].scale = scale;
+  } else if (p.ngroups >= 1) {
+    p.groups[p.ngroups - 1].scale = scale;
+  }
   return LFG_OK;
 }
 

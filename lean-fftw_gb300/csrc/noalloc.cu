@@ -92,6 +92,10 @@ extern "C" lfg_status lfg_execute_inplace_static(const lfg_plan* plan, void* dat
     return LFG_ERR_UNSUPPORTED;
   }
   if (p.empty) return LFG_OK;
+  if (!p.stages.empty() || p.howmany2 > 1) {
+    lfg::set_last_error("static-scratch execution takes 1-D plans with one batch dimension");
+    return LFG_ERR_UNSUPPORTED;
+  }
   const size_t es = p.precision == 0 ? 16 : 8;
   const size_t need = (size_t)p.n * (size_t)p.howmany * es;
   if (p.ngroups == 2 && need > kStaticScratchBytes) {

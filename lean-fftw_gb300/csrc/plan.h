@@ -2,16 +2,19 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
+#include "r2r.h"
 #include "real.h"
 #include "stockham.h"
 
 namespace lfg {
 
-enum class Kind { C2C, R2C, C2R };
+enum class Kind { C2C, R2C, C2R, R2R };
 
 // Layout of one side (input or output) of a batched 1-D transform, in complex (C2C) or real
 // elements of the side's scalar type, relative to the pointer given at execution.
@@ -21,6 +24,16 @@ struct Side {
   int64_t dist = 0;      // between consecutive lines
 };
 
+struct Plan;
+
+// One axis of a multi-axis complex plan: a 1-D plan along the axis over the other dimensions,
+// launched once per entry of `loops` (input and output element offsets of batch dimensions
+// beyond the two a launch covers).
+struct AxisStage {
+  std::shared_ptr<Plan> plan;
+  std::vector<std::array<int64_t, 2>> loops;
+};
+
 struct Plan {
   Kind kind = Kind::C2C;
   int precision = 0;     // 0: binary64, 1: binary32
@@ -28,6 +41,13 @@ struct Plan {
   int64_t n = 0;         // transform size
   int64_t howmany = 1;
   Side in, out;
+  // a second (outer) batch dimension of a 1-D complex plan: howmany2 blocks of `howmany`
+  // lines, in_dist2 / out_dist2 elements apart
+  int64_t howmany2 = 1;
+  int64_t in_dist2 = 0, out_dist2 = 0;
+  // multi-axis complex plans (rank >= 2, or more vector dimensions than two): the stages run
+  // in order, the first from the input to the output, the others in place on the output
+  std::vector<AxisStage> stages;
   int64_t in_span = 0;   // spanned input and output, in scalars, from the execution pointer
   int64_t out_span = 0;
   std::vector<int> radices;
@@ -63,6 +83,12 @@ struct Plan {
   int64_t col_in_off = 0;        // c2r rank 2: complex offset of the input's first element
   void* d_post = nullptr;
   void* d_col_twiddles = nullptr;
+  // real-to-real lines (kind R2R): embedding descriptor, the complex DFT of the embedding
+  // size over all lines (none when that size is 1), and the plan's two complex buffers
+  // (embedding, spectrum) of lines x M elements each
+  R2RDesc r2r{};
+  std::shared_ptr<Plan> r2r_dft;
+  void* d_r2r_buf = nullptr;
 };
 
 // Geometry of a real transform: vector count `howmany`, rank-2 size n0 x n (rank 1: n0 = 1).

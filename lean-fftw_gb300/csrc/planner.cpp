@@ -113,9 +113,16 @@ void free_plan_memory(Plan& p) {
   if (p.d_post) cudaFree(p.d_post);
   if (p.d_col_twiddles) cudaFree(p.d_col_twiddles);
   if (p.d_status) cudaFree(p.d_status);
+  if (p.d_r2r_buf) cudaFree(p.d_r2r_buf);
+  if (p.r2r_dft) free_plan_memory(*p.r2r_dft);
+  p.r2r_dft.reset();
+  p.d_r2r_buf = nullptr;
   p.d_status = nullptr;
   p.d_twiddles = p.d_scratch = p.d_host_in = p.d_host_out = nullptr;
   p.d_post = p.d_col_twiddles = nullptr;
+  for (AxisStage& s : p.stages)
+    if (s.plan) free_plan_memory(*s.plan);
+  p.stages.clear();
   if (cur != p.device) cudaSetDevice(cur);
 }
 
@@ -319,14 +326,25 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
     // lines may share a tile; pick C by the target only (the batch need not divide)
     int64_t cmax = std::max<int64_t>(1, tile_target / N);
     while (cmax > 1 && smem_bytes(cmax, N, prec) > kSmemBudget) --cmax;
-    g.C = (int)std::min<int64_t>(cmax, std::max<int64_t>(1, p.howmany));
-    g.total_sub = p.howmany;
-    g.in_line = p.in.dist;
-    g.in_sub = 0;
+    const int64_t lines = p.howmany * p.howmany2;
+    g.C = (int)std::min<int64_t>(cmax, std::max<int64_t>(1, lines));
+    g.total_sub = lines;
     g.in_elem = p.in.stride;
-    g.out_line = p.out.dist;
-    g.out_sub = 0;
     g.out_elem = p.out.stride;
+    if (p.howmany2 == 1) {
+      g.in_line = p.in.dist;
+      g.in_sub = 0;
+      g.out_line = p.out.dist;
+      g.out_sub = 0;
+    } else {
+      // two batch dimensions: the inner one indexes sub-problems within an outer "line"
+      // (a single group's twiddles do not depend on the sub-problem index)
+      g.nsub = (int)p.howmany;
+      g.in_sub = p.in.dist;
+      g.out_sub = p.out.dist;
+      g.in_line = p.in_dist2;
+      g.out_line = p.out_dist2;
+    }
     p.group_first_pass[0] = 0;
   } else {
     p.ngroups = 2;
@@ -356,7 +374,8 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
       p.groups[gi].pass[t].comp = comp[p.group_first_pass[gi] + t];
   // binary32 over back-to-back lines: the persistent kernel with bulk-copy prefetch
   const GroupDesc& g0 = p.groups[0];
-  if (prec == 1 && p.ngroups == 1 && p.in.stride == 1 && p.out.stride == 1 && p.in.dist == N &&
+  if (prec == 1 && p.ngroups == 1 && p.howmany2 == 1 && p.in.stride == 1 && p.out.stride == 1 &&
+      p.in.dist == N &&
       p.out.dist == N && (N % 2) == 0 && p.howmany > 0 &&
       smem_bytes(g0.C, g0.M, prec) * 2 <= kSmemBudget) {
     if (cudaMalloc(&p.d_status, sizeof(int)) == cudaSuccess &&
@@ -496,9 +515,67 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
   return "";
 }
 
+// The intermediate buffer of in-place two-group execution (one block of lines), allocated on
+// first use and kept by the plan.
+static cudaError_t ensure_scratch(const Plan& p) {
+  const size_t need = (size_t)p.n * (size_t)p.howmany * (p.precision == 0 ? 16 : 8);
+  if (p.scratch_bytes >= need) return cudaSuccess;
+  if (p.d_scratch) cudaFree(p.d_scratch);
+  p.d_scratch = nullptr;
+  p.scratch_bytes = 0;
+  cudaError_t e = cudaMalloc(&p.d_scratch, need);
+  if (e == cudaSuccess) p.scratch_bytes = need;
+  return e;
+}
+
 cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream,
                          bool force_scratch) {
   if (p.empty) return cudaSuccess;
+  if (p.kind == Kind::R2R && p.stages.empty()) {
+    // embedding -> complex DFT of the embedding size -> extraction
+    const size_t ces = p.precision == 0 ? 16 : 8;
+    char* A = static_cast<char*>(p.d_r2r_buf);
+    char* B = A + (size_t)p.r2r.lines * (size_t)p.r2r.M * ces;
+    cudaError_t e = launch_r2r_embed(p.r2r, p.precision, in, A, stream);
+    if (e != cudaSuccess) return e;
+    if (p.r2r_dft) {
+      e = execute_plan(*p.r2r_dft, A, B, stream);
+      if (e != cudaSuccess) return e;
+    } else {
+      B = A;
+    }
+    return launch_r2r_extract(p.r2r, p.precision, B, out, stream);
+  }
+  if (!p.stages.empty()) {
+    // axis by axis: the first stage reads the input, the others work in place on the output
+    const size_t es = p.kind == Kind::R2R ? (p.precision == 0 ? 8 : 4) : (p.precision == 0 ? 16 : 8);
+    for (size_t k = 0; k < p.stages.size(); ++k) {
+      const AxisStage& st = p.stages[k];
+      const char* src = k == 0 ? static_cast<const char*>(in) : static_cast<const char*>(out);
+      for (const auto& off : st.loops) {
+        cudaError_t e = execute_plan(*st.plan, src + off[0] * (int64_t)es,
+                                     static_cast<char*>(out) + off[1] * (int64_t)es, stream,
+                                     force_scratch);
+        if (e != cudaSuccess) return e;
+      }
+    }
+    return cudaSuccess;
+  }
+  if (p.howmany2 > 1 && p.ngroups == 2) {
+    // two pass groups use the sub-problem index themselves: one launch pair per outer block,
+    // sharing the plan's scratch (allocated here, so the blocks never reallocate it)
+    const size_t es = p.precision == 0 ? 16 : 8;
+    cudaError_t e = (in == out || force_scratch) ? ensure_scratch(p) : cudaSuccess;
+    if (e != cudaSuccess) return e;
+    Plan q = p;
+    q.howmany2 = 1;
+    q.stages.clear();
+    for (int64_t j = 0; j < p.howmany2 && e == cudaSuccess; ++j)
+      e = execute_plan(q, static_cast<const char*>(in) + j * p.in_dist2 * (int64_t)es,
+                       static_cast<char*>(out) + j * p.out_dist2 * (int64_t)es, stream,
+                       force_scratch);
+    return e;
+  }
   const size_t es = p.precision == 0 ? 16 : 8;
   auto launch_col = [&](bool fwd, const void* a, void* b) -> cudaError_t {
     if (p.precision == 0) return launch_group_f64(p.col, fwd, a, b, stream);
@@ -544,15 +621,8 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     z_line = p.out.dist;
     z_stride = p.out.stride;
   } else {
-    size_t need = (size_t)p.n * (size_t)p.howmany * es;
-    if (p.scratch_bytes < need) {
-      if (p.d_scratch) cudaFree(p.d_scratch);
-      p.d_scratch = nullptr;
-      p.scratch_bytes = 0;
-      cudaError_t e = cudaMalloc(&p.d_scratch, need);
-      if (e != cudaSuccess) return e;
-      p.scratch_bytes = need;
-    }
+    cudaError_t e = ensure_scratch(p);
+    if (e != cudaSuccess) return e;
     zb = static_cast<char*>(p.d_scratch);
     z_line = p.n;
     z_stride = 1;

@@ -63,10 +63,15 @@ inline int fastdiv_host(int n, FastDiv f) {
 
 // Shared-memory tile layout: sub-problem c of a tile starts at c * sub_pitch(M), and its
 // element i sits at i + i/16 (one padding element after every 16).  The padding spreads a
-// pass's stride-R stores over the banks; the odd pitch puts neighbouring sub-problems in
-// different banks (tile copies of strided sub-problems and passes with fewer than 32
-// butterflies per sub-problem walk across sub-problems).
-LFG_HD constexpr int sub_pitch(int M) { return (M + (M >> 4)) | 1; }
+// pass's stride-R stores over the banks.  Across sub-problems: a warp of a pass whose
+// sub-problems hold few butterflies spans several sub-problems at element stride 17, which
+// the pitch M + M/16 (= 17 M/16) keeps conflict-free for M a multiple of 16; for other M an
+// odd pitch puts neighbouring sub-problems in different banks.  (An odd pitch for large
+// multiples of 16 removes the conflicts of strided tile copies too, but measured slower on
+// the binary32 stream kernel and no faster elsewhere.)
+LFG_HD constexpr int sub_pitch(int M) {
+  return (M & 15) == 0 ? M + (M >> 4) : (M + (M >> 4)) | 1;
+}
 LFG_HD constexpr int64_t tile_elems(int64_t C, int M) { return C * (int64_t)sub_pitch(M); }
 
 struct PassDesc {

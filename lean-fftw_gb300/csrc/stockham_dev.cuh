@@ -53,15 +53,27 @@ __device__ __forceinline__ int fdiv(int n, const FastDiv& f) {
   return (int)((__umulhi(f.m, (unsigned)n) + (unsigned)n) >> f.l);
 }
 
-// One pass over the C sub-problems of a tile: src, dst are tile buffers in shared memory
-// (dst padded; src padded unless SRCPAD is false, as for a stage buffer a bulk copy filled).
+// Destination of a pass's outputs: the next shared-memory tile buffer (padded layout).  A
+// pass takes it as a policy object (row(c): start of sub-problem c; put: one output).
+template <class T>
+struct SmemOut {
+  typename Prec<T>::C* dst;
+  int pitch;
+  __device__ __forceinline__ typename Prec<T>::C* row(int c) const { return dst + c * pitch; }
+  __device__ __forceinline__ void put(typename Prec<T>::C* row, int i, typename Prec<T>::C v) const {
+    row[spad(i)] = v;
+  }
+};
+
+// One pass over the C sub-problems of a tile: src is a tile buffer in shared memory (padded
+// unless SRCPAD is false, as for a stage buffer a bulk copy filled); outputs go to `out`.
 // MODE 0: untwiddled; 1: twiddled codelet (table twiddles); 2: compensated twiddle products
 // with (hi, lo) binary32 twiddles, then the untwiddled codelet.
 // sub0: index within its line of the tile's first sub-problem (second group), else -1.
-template <class T, bool FWD, int R, int MODE, bool SRCPAD = true>
+template <class T, bool FWD, int R, int MODE, bool SRCPAD, class Out>
 __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ src,
-                                       typename Prec<T>::C* __restrict__ dst, int C, int M,
-                                       const PassDesc& pd, int kmul, int sub0, int nsub,
+                                       const Out& out, int C, int M,
+                                       const PassDesc& pd, int sub0, int nsub,
                                        const FastDiv& fd_nsub) {
   using P = Prec<T>;
   using Cx = typename P::C;
@@ -109,31 +121,31 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
       for (int r = 1; r < R; ++r) {
         const T wrh = __ldg(tw + 2 * (r - 1) * nsg + kg), wih = __ldg(tw + (2 * r - 1) * nsg + kg);
         const T wrl = __ldg(lo + 2 * (r - 1) * nsg + kg), wil = __ldg(lo + (2 * r - 1) * nsg + kg);
-        const T a = x[2 * r], b = x[2 * r + 1];
-        const T cr = P::fma(a, wrl, -P::mul(b, wil));          // small correction terms
-        const T ci = P::fma(a, wil, P::mul(b, wrl));
-        x[2 * r] = P::fma(a, wrh, P::fma(-b, wih, cr));
-        x[2 * r + 1] = P::fma(a, wih, P::fma(b, wrh, ci));
+        const T a = x[2 * r], bi = x[2 * r + 1];
+        const T cr = P::fma(a, wrl, -P::mul(bi, wil));          // small correction terms
+        const T ci = P::fma(a, wil, P::mul(bi, wrl));
+        x[2 * r] = P::fma(a, wrh, P::fma(-bi, wih, cr));
+        x[2 * r + 1] = P::fma(a, wih, P::fma(bi, wrh, ci));
       }
     }
     P::template Bfly<FWD, R, TW>::run(x, y);
     const int d0 = b * ns * R + k;
-    Cx* dc = dst + c * PM;
+    Cx* dc = out.row(c);
 #pragma unroll
-    for (int r = 0; r < R; ++r) dc[spad(d0 + r * ns)] = P::mk(y[2 * r], y[2 * r + 1]);
+    for (int r = 0; r < R; ++r) out.put(dc, d0 + r * ns, P::mk(y[2 * r], y[2 * r + 1]));
   }
 }
 
-template <class T, bool FWD, bool SRCPAD = true>
-__device__ __forceinline__ void run_pass_t(const typename Prec<T>::C* src, typename Prec<T>::C* dst,
-                                           int C, int M, const PassDesc& pd, int kmul,
-                                           int sub0, int nsub, const FastDiv& fd_nsub) {
+template <class T, bool FWD, bool SRCPAD = true, class Out>
+__device__ __forceinline__ void run_pass_to(const typename Prec<T>::C* src, const Out& out,
+                                            int C, int M, const PassDesc& pd, int sub0, int nsub,
+                                            const FastDiv& fd_nsub) {
 #define LFG_PASS_CASE(RR)                                                                        \
   case RR:                                                                                       \
-    if (!pd.tw) pass_t<T, FWD, RR, 0, SRCPAD>(src, dst, C, M, pd, kmul, sub0, nsub, fd_nsub);    \
+    if (!pd.tw) pass_t<T, FWD, RR, 0, SRCPAD>(src, out, C, M, pd, sub0, nsub, fd_nsub);          \
     else if (sizeof(T) == 4 && pd.comp)                                                          \
-      pass_t<T, FWD, RR, 2, SRCPAD>(src, dst, C, M, pd, kmul, sub0, nsub, fd_nsub);              \
-    else pass_t<T, FWD, RR, 1, SRCPAD>(src, dst, C, M, pd, kmul, sub0, nsub, fd_nsub);           \
+      pass_t<T, FWD, RR, 2, SRCPAD>(src, out, C, M, pd, sub0, nsub, fd_nsub);                    \
+    else pass_t<T, FWD, RR, 1, SRCPAD>(src, out, C, M, pd, sub0, nsub, fd_nsub);                 \
     break;
   switch (pd.R) {
     LFG_PASS_CASE(2)
@@ -154,6 +166,14 @@ __device__ __forceinline__ void run_pass_t(const typename Prec<T>::C* src, typen
     default: break;   // rejected by the planner
   }
 #undef LFG_PASS_CASE
+}
+
+// A pass from one shared-memory tile buffer to another.
+template <class T, bool FWD, bool SRCPAD = true>
+__device__ __forceinline__ void run_pass_t(const typename Prec<T>::C* src, typename Prec<T>::C* dst,
+                                           int C, int M, const PassDesc& pd, int sub0, int nsub,
+                                           const FastDiv& fd_nsub) {
+  run_pass_to<T, FWD, SRCPAD>(src, SmemOut<T>{dst, sub_pitch(M)}, C, M, pd, sub0, nsub, fd_nsub);
 }
 
 // Line bases (complex-element offsets of each line) of the two tile sources: evenly strided
@@ -247,7 +267,7 @@ __device__ __forceinline__ typename Prec<T>::C* run_passes(const GroupDesc& g,
   const int sub0 = msub0 >= 0 ? (int)(msub0 % g.nsub) : -1;
   const FastDiv fd_nsub = g.fd_nsub;
   for (int t = 0; t < npass; ++t) {
-    run_pass_t<T, FWD>(A, B, C, g.M, g.pass[t], g.kmul, sub0, g.nsub, fd_nsub);
+    run_pass_t<T, FWD>(A, B, C, g.M, g.pass[t], sub0, g.nsub, fd_nsub);
     __syncthreads();
     auto tmp = A;
     A = B;

@@ -79,7 +79,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 // A wait that gives up sets *status = 1, waits (bounded) for this CTA's copies in flight and
 // returns.
 template <bool FWD>
-__global__ void __launch_bounds__(kGroupThreads)
+__global__ void __launch_bounds__(kGroupThreads, 3)
 stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __restrict__ out,
                   int64_t lines, int* status) {
   extern __shared__ __align__(128) float2 smem_f32s[];
@@ -123,8 +123,8 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
     float2* src = smem_f32s + s * CM;
     float2* dst = A;
     for (int t = 0; t < g.npass; ++t) {
-      if (t == 0) run_pass_t<float, FWD, false>(src, dst, C, M, g.pass[t], g.kmul, -1, g.nsub, g.fd_nsub);
-      else run_pass_t<float, FWD>(src, dst, C, M, g.pass[t], g.kmul, -1, g.nsub, g.fd_nsub);
+      if (t == 0) run_pass_t<float, FWD, false>(src, dst, C, M, g.pass[t], -1, g.nsub, g.fd_nsub);
+      else run_pass_t<float, FWD>(src, dst, C, M, g.pass[t], -1, g.nsub, g.fd_nsub);
       __syncthreads();
       if (t == 0) {
         // the stage buffer has been read: refill it with this CTA's tile kStages ahead
@@ -143,10 +143,19 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
     float4* o4 = reinterpret_cast<float4*>(out + l0 * M);
     const int n4 = C * M / 2;
     const float sc = (float)g.scale;
+    const bool flat = (M & 15) == 0;   // then c * PM + spad(ii) = spad(c * M + ii)
     for (int i = threadIdx.x; i < n4; i += blockDim.x) {
-      const int e = 2 * i, c = fdiv(e, g.fd_m), ii = e - c * M;   // M even: ii + 1 < M
-      const float2* row = src + c * PM;
-      const float2 a = row[spad(ii)], b = row[spad(ii + 1)];
+      const int e = 2 * i;
+      int t0, t1;
+      if (flat) {
+        t0 = spad(e);
+        t1 = spad(e + 1);
+      } else {
+        const int c = fdiv(e, g.fd_m), ii = e - c * M;   // M even: ii + 1 < M
+        t0 = c * PM + spad(ii);
+        t1 = c * PM + spad(ii + 1);
+      }
+      const float2 a = src[t0], b = src[t1];
       if (g.scale == 1.0) o4[i] = make_float4(a.x, a.y, b.x, b.y);
       else o4[i] = make_float4(__fmul_rn(a.x, sc), __fmul_rn(a.y, sc), __fmul_rn(b.x, sc), __fmul_rn(b.y, sc));
     }
@@ -221,7 +230,7 @@ tile_stream_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
     cp_async_wait_all();
     __syncthreads();
     const int sub0 = g.twsub ? (int)(s0 % g.nsub) : -1;
-    run_pass_t<float, FWD>(S, A, C, g.M, g.pass[0], g.kmul, sub0, g.nsub, g.fd_nsub);
+    run_pass_t<float, FWD>(S, A, C, g.M, g.pass[0], sub0, g.nsub, g.fd_nsub);
     __syncthreads();
     // the stage buffer has been consumed: start copying this CTA's next tile
     const int64_t next = tile + gridDim.x;
@@ -229,7 +238,7 @@ tile_stream_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
     float2* src = A;
     float2* dst = B;
     for (int t = 1; t < g.npass; ++t) {
-      run_pass_t<float, FWD>(src, dst, C, g.M, g.pass[t], g.kmul, sub0, g.nsub, g.fd_nsub);
+      run_pass_t<float, FWD>(src, dst, C, g.M, g.pass[t], sub0, g.nsub, g.fd_nsub);
       __syncthreads();
       float2* tmp = src;
       src = dst;

@@ -55,6 +55,8 @@ _SIG = {
     "lfg_plan_1d_radices": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t,
                                             ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                             ctypes.POINTER(_VP)]),
+    "lfg_plan_r2r": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t, ctypes.c_int,
+                                    ctypes.c_uint, ctypes.POINTER(ctypes.c_void_p)]),
     "lfg_plan_r2c": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint,
                                      ctypes.POINTER(_VP)]),
     "lfg_plan_c2r": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_uint,

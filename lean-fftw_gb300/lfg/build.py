@@ -8,6 +8,8 @@
    the planner).
 2. Compiles csrc/*.cu for sm_103a (nvcc -gencode arch=compute_103a,code=sm_103a) and the
    host sources with g++, in parallel, and links lfg/liblfg.so.
+3. Builds the libbench2-style command line lfg/lfg-bench (csrc/tools/lfg_bench.cpp) against
+   liblfg.so.
 """
 from __future__ import annotations
 
@@ -128,9 +130,35 @@ def compile_all(verbose: bool = False, jobs: int = 8) -> str:
     return LIB
 
 
+CLI = os.path.join(PKG, "lfg-bench")
+
+
+def build_cli() -> str:
+    src = os.path.join(CSRC, "tools", "lfg_bench.cpp")
+    stamp = CLI + ".digest"
+    d = _digest([src, LIB, os.path.join(REPO, "include", "lfg.h")])
+    if os.path.exists(CLI) and os.path.exists(stamp) and open(stamp).read() == d:
+        return CLI
+    cuda = cuda_home()
+    tmp = CLI + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", os.path.join(REPO, "include"),
+           "-I", os.path.join(cuda, "include"), src, "-o", tmp, "-L", PKG, "-llfg",
+           "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN",
+           "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    with open(stamp, "w") as f:
+        f.write(d)
+    return CLI
+
+
 def build(verbose: bool = False) -> str:
     generate()
-    return compile_all(verbose=verbose)
+    lib = compile_all(verbose=verbose)
+    build_cli()
+    return lib
 
 
 if __name__ == "__main__":

@@ -129,6 +129,19 @@ def plan_c2r(n: int, howmany: int = 1, precision="f64", adjoint: bool = False) -
     return Plan(h)
 
 
+R2R_KINDS = {"r2hc": 0, "hc2r": 1, "dht": 2, "redft00": 3, "redft01": 4, "redft10": 5,
+             "redft11": 6, "rodft00": 7, "rodft01": 8, "rodft10": 9, "rodft11": 10}
+
+
+def plan_r2r(n: int, kind, howmany: int = 1, precision="f64") -> Plan:
+    """Real-to-real transform of one of the eleven kinds (name or libbench2 number) on
+    `howmany` contiguous lines of n reals (Core/Problem.lean:64-112, 151-163)."""
+    k = R2R_KINDS[kind.lower()] if isinstance(kind, str) else int(kind)
+    h = ctypes.c_void_p()
+    check(lib().lfg_plan_r2r(n, k, howmany, _prec(precision), 0, ctypes.byref(h)))
+    return Plan(h)
+
+
 def plan_r2c_2d(n0: int, n1: int, howmany: int = 1, precision="f64") -> Plan:
     """Rank-2 r2c of n0 x n1 real images to n0 x (n1/2+1) complex (Core/Problem.lean:228-233)."""
     h = ctypes.c_void_p()

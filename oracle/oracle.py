@@ -11,6 +11,11 @@ What is here, and the reference code each piece follows (paths inside lean-fftw)
 * `generic_r2c/c2r`    LineOp.apply for r2c and c2r (Core/Problem.lean:142-150, hermExt :137).
 * `generic_rank2_r2c`  planProblemCore for rdft2 forward, rank 2 (Core/Problem.lean:228-233):
                        r2c along the last axis, then a complex forward DFT along the first.
+* `r2r_embed/extract`  R2RKind.embedSize / embed / extract and the hc2r branch of
+                       LineOp.apply (Core/Problem.lean:64-112, 151-163): exact index maps;
+                       `generic_r2r` (the generic engine's r2r), `fast_r2r` (the same
+                       embedding around refTransform: what the GPU computes, bit for bit),
+                       `dd_r2r` (extended precision).
 * `dd_dft`             extended-precision (double-double) DFT: the accuracy oracle.
 * `lcg_rand`           randArr of scripts/AsmTest.lean:7-13, the reference tests' inputs.
 
@@ -307,3 +312,126 @@ def uniform_complex(shape, seed: int = 20261016) -> np.ndarray:
     rng = np.random.default_rng(seed)
     a = rng.random(tuple(shape) + (2,)) - 0.5
     return a.view(np.complex128).reshape(shape)
+
+
+# ---- real-to-real kinds (Core/Problem.lean:64-112, 151-163) -----------------------------------
+
+R2R_KINDS = ["r2hc", "hc2r", "dht", "redft00", "redft01", "redft10", "redft11",
+             "rodft00", "rodft01", "rodft10", "rodft11"]   # libbench2 numbering (FFI.lean:29-31)
+
+
+def r2r_embed_size(kind: str, n: int) -> int:
+    """embedSize (Problem.lean:66-72)."""
+    if kind in ("r2hc", "hc2r", "dht"):
+        return n
+    if kind == "redft00":
+        return 2 * (n - 1)
+    if kind == "rodft00":
+        return 2 * (n + 1)
+    if kind in ("redft10", "redft01", "rodft10", "rodft01"):
+        return 4 * n
+    return 8 * n
+
+
+def r2r_embed(kind: str, x: np.ndarray) -> np.ndarray:
+    """The complex sequence whose DFT holds the transform (embed, Problem.lean:76-98; for
+    hc2r the Hermitian extension of the halfcomplex input, :153-158); last axis."""
+    n = x.shape[-1]
+    M = r2r_embed_size(kind, n)
+    z = np.zeros(x.shape[:-1] + (M,), dtype=np.complex128)
+    i = np.arange(M)
+    X = lambda j: x[..., j]
+    if kind in ("r2hc", "dht"):
+        z.real[...] = x
+    elif kind == "hc2r":
+        k = np.where(i <= n // 2, i, n - i)
+        ik = np.where((0 < k) & (k < n - k), X(np.where((0 < k) & (k < n - k), n - k, 0)), 0.0)
+        z.real[...] = X(k)
+        z.imag[...] = np.where(i <= n // 2, ik, -ik)
+    elif kind == "redft00":
+        z.real[...] = X(np.where(i < n, i, M - i))
+    elif kind == "rodft00":
+        lo = (1 <= i) & (i <= n)
+        hi = (n + 2 <= i) & (i < M)
+        v = np.where(lo, X(np.clip(i - 1, 0, n - 1)), 0.0)
+        z.real[...] = np.where(hi, -X(np.clip(M - i - 1, 0, n - 1)), v)
+    elif kind in ("redft10", "rodft10"):
+        sgn = 1.0 if kind == "redft10" else -1.0
+        odd = (i % 2) == 1
+        a = X(np.clip(i // 2, 0, n - 1))
+        b = sgn * X(np.clip((M - i) // 2, 0, n - 1))
+        z.real[...] = np.where(odd, np.where(i < 2 * n, a, b), 0.0)
+    elif kind in ("redft11", "rodft11"):
+        sgn = 1.0 if kind == "redft11" else -1.0
+        odd = (i % 2) == 1
+        a = X(np.clip(i // 2, 0, n - 1))
+        b = sgn * X(np.clip((M - i) // 2, 0, n - 1))
+        z.real[...] = np.where(odd & (i < 2 * n), a, np.where(odd & (6 * n < i), b, 0.0))
+    elif kind == "redft01":
+        z.real[...] = np.where(i < n, X(np.clip(i, 0, n - 1)),
+                               np.where((3 * n < i) & (i < M), X(np.clip(M - i, 0, n - 1)), 0.0))
+    elif kind == "rodft01":
+        lo = (1 <= i) & (i <= n)
+        hi = (3 * n < i) & (i < M)
+        z.real[...] = np.where(lo, X(np.clip(i - 1, 0, n - 1)),
+                               np.where(hi, -X(np.clip(M - i - 1, 0, n - 1)), 0.0))
+    else:
+        raise ValueError(kind)
+    return z
+
+
+def r2r_extract(kind: str, n: int, F: np.ndarray) -> np.ndarray:
+    """extract (Problem.lean:101-110) on the last axis of the DFT F of the embedding."""
+    j = np.arange(n)
+    if kind == "r2hc":
+        return np.where(j <= n // 2, F.real[..., np.minimum(j, n - 1)],
+                        F.imag[..., (n - j) % max(n, 1)])
+    if kind in ("hc2r", "redft00", "redft10"):
+        return np.ascontiguousarray(F.real[..., :n])
+    if kind == "dht":
+        return np.ascontiguousarray(F.real[..., :n] - F.imag[..., :n])
+    if kind in ("redft01", "redft11"):
+        return np.ascontiguousarray(F.real[..., 2 * j + 1])
+    if kind in ("rodft00", "rodft10"):
+        return np.ascontiguousarray(-F.imag[..., j + 1])
+    return np.ascontiguousarray(-F.imag[..., 2 * j + 1])
+
+
+def _r2r_dft_fwd(kind: str) -> bool:
+    return kind != "hc2r"
+
+
+def generic_r2r(kind: str, x: np.ndarray, nthreads: int = 1) -> np.ndarray:
+    """The generic engine's r2r line (LineOp.apply, Problem.lean:151-163)."""
+    z = r2r_embed(kind, x)
+    if z.shape[-1] == 1:
+        return r2r_extract(kind, x.shape[-1], z)
+    return r2r_extract(kind, x.shape[-1], generic_dft(_r2r_dft_fwd(kind), z, nthreads))
+
+
+def fast_r2r(kind: str, x: np.ndarray, radices, nthreads: int = 1) -> np.ndarray:
+    """The same embedding around refTransform of the embedding size with `radices`."""
+    z = r2r_embed(kind, x)
+    M = z.shape[-1]
+    if M == 1:
+        return r2r_extract(kind, x.shape[-1], z)
+    return r2r_extract(kind, x.shape[-1], ref_transform(_r2r_dft_fwd(kind), M, radices, z, nthreads))
+
+
+def dd_r2r(kind: str, x: np.ndarray, nthreads: int = 1):
+    """Extended precision: (hi, lo) of the extraction from the double-double DFT (the
+    extraction is exact except DHT's re - im, taken on both parts)."""
+    z = r2r_embed(kind, x)
+    n = x.shape[-1]
+    if z.shape[-1] == 1:
+        return r2r_extract(kind, n, z), np.zeros(x.shape)
+    hi, lo = dd_dft(_r2r_dft_fwd(kind), z, nthreads)
+    if kind == "dht":
+        # re - im with its rounding error kept (TwoSum), so (hi, lo) stays extended
+        a, b = hi.real[..., :n], -hi.imag[..., :n]
+        s = a + b
+        bb = s - a
+        err = (a - (s - bb)) + (b - bb)
+        return np.ascontiguousarray(s), np.ascontiguousarray(err + (lo.real[..., :n] - lo.imag[..., :n]))
+    return r2r_extract(kind, n, hi), r2r_extract(kind, n, lo)
+

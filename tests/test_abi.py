@@ -55,9 +55,12 @@ def test_unsupported_sizes_rejected_before_device_use():
         lfg.plan_1d(17)
     with pytest.raises(lfg.Unsupported):
         lfg.plan_1d(1 << 25)
-    # r2r (kind 2) is outside the GPU path
+    # r2r whose embedding size has a prime factor above 13 (REDFT00 of 18: a DFT of 34), and
+    # REDFT00 of one point (undefined, as in the reference), are refused before any device use
     with pytest.raises(lfg.Unsupported):
-        lfg.plan_spec([2, -1, 1, 0, 0, 0, 0, 0, 16, 1, 1, 0])
+        lfg.plan_spec([2, -1, 1, 0, 0, 0, 0, 0, 18, 1, 1, 3])
+    with pytest.raises(lfg.Unsupported):
+        lfg.plan_r2r(1, "redft00")
 
 
 def test_invalid_arguments():
