@@ -85,8 +85,83 @@ int64_t span_scalars(const lfg::Side& s, int64_t n, int64_t howmany, int64_t per
   return (s.offset + (n - 1) * s.stride + (howmany - 1) * s.dist + 1) * per_elem;
 }
 
+lfg_status build_chirp_device(lfg::Plan& p);
+
+// Prime factors of n in ascending order, with multiplicity (lean-fftw `primeFactors`).
+std::vector<int> prime_factors(int64_t n) {
+  std::vector<int> fs;
+  for (int64_t d = 2; n > 1;) {
+    if (d * d > n) {
+      fs.push_back((int)n);
+      break;
+    }
+    if (n % d == 0) {
+      fs.push_back((int)d);
+      n /= d;
+    } else {
+      ++d;
+    }
+  }
+  return fs;
+}
+
+// Small sizes with a prime factor above 13: the generic engine's own transform (generic.cu),
+// the reference's operations exactly, while its direct sums stay cheap (largest factor
+// <= 1024); larger ones go through Bluestein's identity, which is also more accurate there.
+lfg_status build_generic_device(lfg::Plan& p) {
+  const std::vector<int> fs = prime_factors(p.n);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  p.device = dev;
+  p.generic = true;
+  p.ngroups = 0;
+  if (p.empty) return LFG_OK;
+  if ((e = lfg::prepare_generic_kernels()) != cudaSuccess) return cuda_fail(e, "kernel set-up");
+  lfg::GenericDesc& g = p.gen;
+  g.n = (int)p.n;
+  g.nf = (int)fs.size();
+  int64_t acc = 1;
+  for (int i = g.nf - 1; i >= 0; --i) {
+    g.f[i] = fs[i];
+    acc *= fs[i];
+    g.ni[i] = (int)acc;
+  }
+  g.lines = std::max<int64_t>(1, p.howmany) * std::max<int64_t>(1, p.howmany2);
+  g.nl1 = std::max<int64_t>(1, p.howmany);
+  g.in_stride = p.in.stride;
+  g.in_dist = p.in.dist;
+  g.in_dist2 = p.in_dist2;
+  g.out_stride = p.out.stride;
+  g.out_dist = p.out.dist;
+  g.out_dist2 = p.out_dist2;
+  g.scale = 1.0;
+  const std::vector<double> tab = lfg::cos_sin_2pi_table((uint64_t)p.n);
+  const size_t es = p.precision == 0 ? sizeof(double) : sizeof(float);
+  e = cudaMalloc(&p.d_gen_tab, tab.size() * es);
+  if (e == cudaSuccess) {
+    if (p.precision == 0) {
+      e = cudaMemcpy(p.d_gen_tab, tab.data(), tab.size() * es, cudaMemcpyHostToDevice);
+    } else {
+      std::vector<float> f(tab.begin(), tab.end());
+      e = cudaMemcpy(p.d_gen_tab, f.data(), f.size() * es, cudaMemcpyHostToDevice);
+    }
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "generic twiddle table");
+  g.tab = p.d_gen_tab;
+  double sum = 0;
+  for (int f : fs) sum += f;
+  p.flops = 8.0 * (double)p.n * sum * (double)g.lines;
+  return LFG_OK;
+}
+
 // Device part of a 1-D complex plan: kernels set up, autotuning, groups and tables.
 lfg_status build_c2c_device(lfg::Plan& p) {
+  if (!smooth13(p.n)) {
+    const std::vector<int> fs = prime_factors(p.n);
+    if (p.n <= lfg::kGenericMaxN && fs.back() <= 1024) return build_generic_device(p);
+    return build_chirp_device(p);
+  }
   // binary64 is bound by the FP64 pipe: two groups of small tiles (more CTAs per SM) beat one
   // group with a CTA-sized tile above 2048 points; binary32 is bound by HBM: as few groups as fit
   const bool user_split = p.single_max > 0 || p.tile > 0;
@@ -120,6 +195,123 @@ lfg_status build_c2c_device(lfg::Plan& p) {
       return fail(LFG_ERR_UNSUPPORTED, msg);
     }
   }
+  return LFG_OK;
+}
+
+// Smallest 13-smooth integer >= m.
+int64_t next_smooth(int64_t m) {
+  while (!smooth13(m)) ++m;
+  return m;
+}
+
+// Bluestein plan for a size with a prime factor above 13 (chirp.cu explains the identity):
+// chirp table, the filter's spectrum (computed once, in binary64, by a transform of length
+// L), and forward/backward transforms of length L over all lines of the batch.
+lfg_status build_chirp_device(lfg::Plan& p) {
+  const int64_t n = p.n;
+  if (n < 2 || n > ((int64_t)1 << 24)) return fail(LFG_ERR_UNSUPPORTED, "size outside 2..2^24");
+  const int64_t L = next_smooth(2 * n - 1);
+  const int64_t lines = std::max<int64_t>(1, p.howmany) * std::max<int64_t>(1, p.howmany2);
+  if (lines * L >= ((int64_t)1 << 31))
+    return fail(LFG_ERR_UNSUPPORTED, "batch too large for the chirp-z path (2^31 elements)");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  p.device = dev;
+  p.ngroups = 0;
+  if (p.empty) return LFG_OK;
+  // chirp c_m = exp(s pi i m^2 / n) = cos/sin(2 pi t / 2n), t = m^2 mod 2n (exact table)
+  const std::vector<double> tab = lfg::cos_sin_2pi_table((uint64_t)(2 * n));
+  const double sg = p.fwd ? -1.0 : 1.0;
+  std::vector<double> c(2 * n), b(2 * L, 0.0);
+  for (int64_t m = 0; m < n; ++m) {
+    const int64_t t = (m * m) % (2 * n);   // m < 2^24: no overflow
+    c[2 * m] = tab[2 * t];
+    c[2 * m + 1] = sg * tab[2 * t + 1];
+    // the filter conj(c_m) at m and at L - m
+    b[2 * m] = c[2 * m];
+    b[2 * m + 1] = -c[2 * m + 1];
+    if (m > 0) {
+      b[2 * (L - m)] = c[2 * m];
+      b[2 * (L - m) + 1] = -c[2 * m + 1];
+    }
+  }
+  // its forward transform in binary64
+  std::vector<double> bh(2 * L);
+  {
+    lfg::Plan t;
+    t.kind = lfg::Kind::C2C;
+    t.precision = 0;
+    t.fwd = true;
+    t.n = L;
+    t.howmany = 1;
+    t.in = t.out = {0, 1, L};
+    t.radices = lfg::choose_radices(L, 0);
+    lfg_status s = build_c2c_device(t);
+    if (s != LFG_OK) return s;
+    void* db = nullptr;
+    e = cudaMalloc(&db, 2 * 2 * L * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(db, b.data(), 2 * L * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = lfg::execute_plan(t, db, static_cast<double*>(db) + 2 * L, nullptr);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(bh.data(), static_cast<double*>(db) + 2 * L, 2 * L * sizeof(double),
+                     cudaMemcpyDeviceToHost);
+    if (db) cudaFree(db);
+    lfg::free_plan_memory(t);
+    if (e != cudaSuccess) return cuda_fail(e, "chirp filter transform");
+  }
+  // chirp and filter spectrum on the device, in the plan's precision
+  const size_t es = p.precision == 0 ? sizeof(double) : sizeof(float);
+  e = cudaMalloc(&p.d_chirp_tab, 2 * (size_t)(n + L) * es);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc of the chirp tables");
+  std::vector<double> both(c);
+  both.insert(both.end(), bh.begin(), bh.end());
+  if (p.precision == 0) {
+    e = cudaMemcpy(p.d_chirp_tab, both.data(), both.size() * es, cudaMemcpyHostToDevice);
+  } else {
+    std::vector<float> f(both.begin(), both.end());
+    e = cudaMemcpy(p.d_chirp_tab, f.data(), f.size() * es, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "chirp table upload");
+  // forward and backward transforms of length L over all lines (dense, out of place)
+  for (int dir = 0; dir < 2; ++dir) {
+    auto q = std::make_shared<lfg::Plan>();
+    q->kind = lfg::Kind::C2C;
+    q->precision = p.precision;
+    q->fwd = dir == 0;
+    q->n = L;
+    q->howmany = lines;
+    q->in = q->out = {0, 1, L};
+    q->no_comp = p.no_comp;
+    q->radices = lfg::choose_radices(L, p.precision);
+    lfg_status s = build_c2c_device(*q);
+    if (s != LFG_OK) return s;
+    if (dir == 1 && q->ngroups >= 1) q->groups[q->ngroups - 1].scale = 1.0 / (double)L;
+    (dir == 0 ? p.chirp_fwd : p.chirp_bwd) = q;
+  }
+  const size_t ces = p.precision == 0 ? 16 : 8;
+  e = cudaMalloc(&p.d_chirp_buf, 2 * (size_t)lines * (size_t)L * ces);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc of the chirp buffers");
+  lfg::ChirpDesc& d = p.chirp;
+  d.n = n;
+  d.L = L;
+  d.lines = lines;
+  d.nl1 = std::max<int64_t>(1, p.howmany);
+  d.in_off = d.out_off = 0;
+  d.in_stride = p.in.stride;
+  d.in_dist = p.in.dist;
+  d.in_dist2 = p.in_dist2;
+  d.out_stride = p.out.stride;
+  d.out_dist = p.out.dist;
+  d.out_dist2 = p.out_dist2;
+  d.fd_L = lfg::make_fastdiv((int)L);
+  d.fd_n = lfg::make_fastdiv((int)n);
+  d.fd_nl1 = lfg::make_fastdiv((int)d.nl1);
+  d.chirp = p.d_chirp_tab;
+  d.bhat = static_cast<const char*>(p.d_chirp_tab) + 2 * (size_t)n * es;
+  p.radices = p.chirp_fwd->radices;
+  p.flops = 2 * p.chirp_fwd->flops + 18.0 * (double)(lines * L);
   return LFG_OK;
 }
 
@@ -177,6 +369,7 @@ lfg_status plan_real_common(bool r2c, size_t n0, size_t n, size_t howmany, lfg_p
   *out = nullptr;
   if (precision != LFG_F64 && precision != LFG_F32) return fail(LFG_ERR_INVALID, "bad precision");
   if (n < 2 || n0 < 1) return fail(LFG_ERR_UNSUPPORTED, "sizes must be >= 2 (last) and >= 1");
+  if (n & 1) return fail(LFG_ERR_UNSUPPORTED, "odd-length real transforms are not executed");
   if (!smooth13((int64_t)n) || !smooth13((int64_t)n0))
     return fail(LFG_ERR_UNSUPPORTED, "sizes must be 13-smooth");
   lfg::Plan p;
@@ -204,7 +397,8 @@ lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision prec
   if (sign != -1 && sign != 1) return fail(LFG_ERR_INVALID, "sign must be -1 or +1");
   if (precision != LFG_F64 && precision != LFG_F32) return fail(LFG_ERR_INVALID, "bad precision");
   if (n < 2 || n > ((size_t)1 << 24)) return fail(LFG_ERR_UNSUPPORTED, "size outside 2..2^24");
-  if (!smooth13((int64_t)n)) return fail(LFG_ERR_UNSUPPORTED, "size has a prime factor above 13");
+  if (radices && !smooth13((int64_t)n))
+    return fail(LFG_ERR_UNSUPPORTED, "explicit radix sequences need a 13-smooth size");
   lfg::Plan p;
   p.kind = lfg::Kind::C2C;
   p.precision = precision;
@@ -237,9 +431,8 @@ lfg_status build_r2r_child(lfg::Plan& c, int rkind, int64_t n, int64_t is, int64
                            unsigned flags) {
   const int64_t M = lfg::r2r_embed_size(rkind, n);
   if (M == 0) return fail(LFG_ERR_UNSUPPORTED, "r2r kind or size not defined (REDFT00 needs n >= 2)");
-  if (M > 1 && (M > ((int64_t)1 << 24) || !smooth13(M)))
-    return fail(LFG_ERR_UNSUPPORTED, "r2r embedding size " + std::to_string(M) +
-                                         " must be 13-smooth and at most 2^24");
+  if (M > ((int64_t)1 << 24))
+    return fail(LFG_ERR_UNSUPPORTED, "r2r embedding size " + std::to_string(M) + " above 2^24");
   const int64_t lines = inner.n * outer.n;
   if (lines * M >= ((int64_t)1 << 31) || lines * n >= ((int64_t)1 << 31))
     return fail(LFG_ERR_UNSUPPORTED, "r2r batch too large (2^31 embedded elements per plan)");
@@ -297,10 +490,10 @@ lfg_status build_r2r_child(lfg::Plan& c, int rkind, int64_t n, int64_t is, int64
 // innermost remaining ones are covered by one launch (lines, and blocks of lines), any
 // further ones by a host loop of launches.  The first stage reads the input; the later
 // stages work in place on the output.  Units: complex elements (c2c) or real scalars (r2r).
-lfg_status plan_separable(bool r2r, const std::vector<CDim>& T, const std::vector<CDim>& V,
-                          const std::vector<int>& kinds, int64_t in_off, int64_t out_off,
-                          int sign, lfg_precision precision, unsigned flags, lfg_plan** out) {
-  lfg::Plan p;
+lfg_status build_separable(lfg::Plan& p, bool r2r, const std::vector<CDim>& T,
+                           const std::vector<CDim>& V, const std::vector<int>& kinds,
+                           int64_t in_off, int64_t out_off, int sign, lfg_precision precision,
+                           unsigned flags) {
   p.kind = r2r ? lfg::Kind::R2R : lfg::Kind::C2C;
   p.precision = precision;
   p.fwd = sign < 0;
@@ -401,6 +594,10 @@ lfg_status plan_separable(bool r2r, const std::vector<CDim>& T, const std::vecto
   const int64_t per = r2r ? 1 : 2;
   p.in_span = per * (ihi + 1);
   p.out_span = per * (ohi + 1);
+  return LFG_OK;
+}
+
+lfg_status wrap_plan(lfg::Plan& p, lfg_plan** out) {
   lfg_plan* h = new (std::nothrow) lfg_plan;
   if (!h) {
     lfg::free_plan_memory(p);
@@ -409,6 +606,219 @@ lfg_status plan_separable(bool r2r, const std::vector<CDim>& T, const std::vecto
   h->p = p;
   *out = h;
   return LFG_OK;
+}
+
+lfg_status plan_separable(bool r2r, const std::vector<CDim>& T, const std::vector<CDim>& V,
+                          const std::vector<int>& kinds, int64_t in_off, int64_t out_off,
+                          int sign, lfg_precision precision, unsigned flags, lfg_plan** out) {
+  lfg::Plan p;
+  lfg_status s = build_separable(p, r2r, T, V, kinds, in_off, out_off, sign, precision, flags);
+  if (s != LFG_OK) return s;
+  return wrap_plan(p, out);
+}
+
+// ---- problems through dense buffers (gather, inner plans, scatter) --------------------------
+
+// Dense row-major complex dimensions (complex units) of extents ns, as CDims.
+std::vector<CDim> dense_dims(const std::vector<int64_t>& ns) {
+  std::vector<CDim> d(ns.size());
+  int64_t acc = 1;
+  for (int k = (int)ns.size() - 1; k >= 0; --k) {
+    d[k] = CDim{ns[k], acc, acc};
+    acc *= ns[k];
+  }
+  return d;
+}
+
+lfg::PackDesc pack_desc(int mode, const std::vector<int64_t>& ns, const std::vector<int64_t>& st,
+                        int64_t re_off, int64_t im_off, int64_t half, int64_t total) {
+  lfg::PackDesc d{};
+  d.ndims = (int)ns.size();
+  d.mode = mode;
+  for (size_t k = 0; k < ns.size(); ++k) {
+    d.n[k] = ns[k];
+    d.st[k] = st[k];
+  }
+  d.re_off = re_off;
+  d.im_off = im_off;
+  d.half = half;
+  d.total = total;
+  return d;
+}
+
+// Highest scalar offset reached from base `off` over extents ns with strides st; -1 if some
+// offset would be negative.
+int64_t reach(int64_t off, const std::vector<int64_t>& ns, const std::vector<int64_t>& st) {
+  int64_t lo = off, hi = off;
+  for (size_t k = 0; k < ns.size(); ++k)
+    if (ns[k] > 1) {
+      const int64_t e = (ns[k] - 1) * st[k];
+      (e > 0 ? hi : lo) += e;
+    }
+  return lo < 0 ? -1 : hi;
+}
+
+// A dimension of the FFI spec in real scalars (any sign of stride).
+struct SDim {
+  int64_t n, is, os;
+};
+
+// Complex DFT of any layout: gather to dense, transform there, scatter.
+lfg_status plan_c2c_packed(const std::vector<SDim>& T, const std::vector<SDim>& V, int64_t inRe,
+                           int64_t inIm, int64_t outRe, int64_t outIm, int sign,
+                           lfg_precision precision, unsigned flags, lfg_plan** out) {
+  std::vector<int64_t> ns, is, os;
+  for (const SDim& d : V) ns.push_back(d.n), is.push_back(d.is), os.push_back(d.os);
+  for (const SDim& d : T) ns.push_back(d.n), is.push_back(d.is), os.push_back(d.os);
+  if ((int)ns.size() > lfg::kPackMaxDims) return fail(LFG_ERR_UNSUPPORTED, "more than 8 dimensions");
+  int64_t total = 1;
+  for (int64_t n : ns) total *= n;
+  lfg::Plan p;
+  p.kind = lfg::Kind::C2C;
+  p.precision = precision;
+  p.fwd = sign < 0;
+  p.empty = total == 0;
+  p.n = 1;
+  for (const SDim& d : T) p.n *= d.n;
+  p.howmany = p.n > 0 ? total / std::max<int64_t>(1, p.n) : 0;
+  const int64_t ih = std::max(reach(inRe, ns, is), reach(inIm, ns, is));
+  const int64_t oh = std::max(reach(outRe, ns, os), reach(outIm, ns, os));
+  if (reach(inRe, ns, is) < 0 || reach(inIm, ns, is) < 0 || reach(outRe, ns, os) < 0 ||
+      reach(outIm, ns, os) < 0)
+    return fail(LFG_ERR_UNSUPPORTED, "strides reach below the buffer start");
+  p.in_span = ih + 1;
+  p.out_span = oh + 1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  p.device = dev;
+  if (!p.empty) {
+    std::vector<int64_t> tn;
+    for (const SDim& d : T) tn.push_back(d.n);
+    const std::vector<CDim> dd = dense_dims(ns);
+    std::vector<CDim> Vd(dd.begin(), dd.begin() + V.size()), Td(dd.begin() + V.size(), dd.end());
+    auto inner = std::make_shared<lfg::Plan>();
+    lfg_status s = build_separable(*inner, false, Td, Vd, {}, 0, 0, sign, precision, flags);
+    if (s != LFG_OK) return s;
+    p.pack_elems = total;
+    const size_t ces = precision == 0 ? 16 : 8;
+    if (cudaMalloc(&p.d_pack_buf, 2 * (size_t)total * ces) != cudaSuccess) {
+      lfg::free_plan_memory(*inner);
+      return fail(LFG_ERR_NOMEM, "cudaMalloc of the dense buffers");
+    }
+    p.steps.push_back({lfg::PackStep::kGather,
+                       pack_desc(lfg::kPackComplex, ns, is, inRe, inIm, 0, total), nullptr, 0, 2});
+    p.steps.push_back({lfg::PackStep::kPlan, {}, inner, 2, 3});
+    p.steps.push_back({lfg::PackStep::kScatter,
+                       pack_desc(lfg::kPackComplex, ns, os, outRe, outIm, 0, total), nullptr, 3, 1});
+    p.flops = inner->flops;
+    p.radices = inner->radices;
+  }
+  return wrap_plan(p, out);
+}
+
+// rdft2 of any layout (rank >= 1; odd, non-smooth or strided sizes; split complex side), as the
+// generic engine computes it (Core/Problem.lean:142-150, 222-236): r2c = the complex forward
+// transform of the real data (imaginary parts 0) over every axis, first n/2+1 values of the
+// last; c2r = complex backward transforms along the other axes of the half spectrum, then the
+// Hermitian extension along the last axis, its backward transform, real parts.
+lfg_status plan_rdft2_packed(bool r2c, const std::vector<SDim>& T, const std::vector<SDim>& V,
+                             int64_t rRe, int64_t cRe, int64_t cIm, lfg_precision precision,
+                             unsigned flags, lfg_plan** out) {
+  const int r = (int)T.size();
+  std::vector<int64_t> ns, rst, cst;   // full extents; real-side and complex-side strides
+  for (const SDim& d : V) {
+    ns.push_back(d.n);
+    rst.push_back(r2c ? d.is : d.os);
+    cst.push_back(r2c ? d.os : d.is);
+  }
+  for (const SDim& d : T) {
+    ns.push_back(d.n);
+    rst.push_back(r2c ? d.is : d.os);
+    cst.push_back(r2c ? d.os : d.is);
+  }
+  if ((int)ns.size() > lfg::kPackMaxDims) return fail(LFG_ERR_UNSUPPORTED, "more than 8 dimensions");
+  const int64_t nl = T[r - 1].n, h = nl / 2 + 1;
+  std::vector<int64_t> hs = ns;
+  hs.back() = h;
+  int64_t total = 1, htotal = 1;
+  for (int64_t n : ns) total *= n;
+  for (int64_t n : hs) htotal *= n;
+  const int64_t rreach = reach(rRe, ns, rst);
+  const int64_t creach = std::max(reach(cRe, hs, cst), reach(cIm, hs, cst));
+  if (rreach < 0 || reach(cRe, hs, cst) < 0 || reach(cIm, hs, cst) < 0)
+    return fail(LFG_ERR_UNSUPPORTED, "strides reach below the buffer start");
+  lfg::Plan p;
+  p.kind = r2c ? lfg::Kind::R2C : lfg::Kind::C2R;
+  p.precision = precision;
+  p.fwd = r2c;
+  p.empty = total == 0;
+  p.n = nl;
+  p.in_span = (r2c ? rreach : creach) + 1;
+  p.out_span = (r2c ? creach : rreach) + 1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  p.device = dev;
+  if (p.empty) return wrap_plan(p, out);
+  const size_t ces = precision == 0 ? 16 : 8;
+  p.pack_elems = total;
+  if (cudaMalloc(&p.d_pack_buf, 2 * (size_t)total * ces) != cudaSuccess)
+    return fail(LFG_ERR_NOMEM, "cudaMalloc of the dense buffers");
+  const int nv = (int)V.size();
+  auto fail_free = [&](lfg_status s) {
+    lfg::free_plan_memory(p);
+    return s;
+  };
+  if (r2c) {
+    const std::vector<CDim> dd = dense_dims(ns);
+    std::vector<CDim> Vd(dd.begin(), dd.begin() + nv), Td(dd.begin() + nv, dd.end());
+    auto inner = std::make_shared<lfg::Plan>();
+    lfg_status s = build_separable(*inner, false, Td, Vd, {}, 0, 0, -1, precision, flags);
+    if (s != LFG_OK) return fail_free(s);
+    p.steps.push_back({lfg::PackStep::kGather, pack_desc(lfg::kPackReal, ns, rst, rRe, -1, 0, total),
+                       nullptr, 0, 2});
+    p.steps.push_back({lfg::PackStep::kPlan, {}, inner, 2, 3});
+    p.steps.push_back({lfg::PackStep::kScatter,
+                       pack_desc(lfg::kPackComplex, ns, cst, cRe, cIm, h, htotal), nullptr, 3, 1});
+    p.flops = inner->flops;
+  } else {
+    // half spectrum, dense (extents hs) in buffer 2
+    p.steps.push_back({lfg::PackStep::kGather, pack_desc(lfg::kPackComplex, hs, cst, cRe, cIm, 0, htotal),
+                       nullptr, 0, 2});
+    bool cols = false;
+    for (int k = 0; k + 1 < r; ++k) cols = cols || T[k].n > 1;
+    if (cols) {
+      // backward transforms along axes 0..r-2 of the half spectrum, in place
+      const std::vector<CDim> dd = dense_dims(hs);
+      std::vector<CDim> Vd(dd.begin(), dd.begin() + nv), Td(dd.begin() + nv, dd.end() - 1);
+      Vd.push_back(dd.back());
+      auto inner = std::make_shared<lfg::Plan>();
+      lfg_status s = build_separable(*inner, false, Td, Vd, {}, 0, 0, 1, precision, flags);
+      if (s != LFG_OK) return fail_free(s);
+      p.steps.push_back({lfg::PackStep::kPlan, {}, inner, 2, 2});
+      p.flops += inner->flops;
+    }
+    // Hermitian extension along the last axis (dense half -> dense full, buffer 3)
+    std::vector<int64_t> hst(hs.size());
+    {
+      int64_t acc = 1;
+      for (int k = (int)hs.size() - 1; k >= 0; --k) {
+        hst[k] = 2 * acc;
+        acc *= hs[k];
+      }
+    }
+    p.steps.push_back({lfg::PackStep::kGather, pack_desc(lfg::kPackHerm, ns, hst, 0, 1, h, total),
+                       nullptr, 2, 3});
+    // backward transform of every row of the last axis, then the real parts
+    auto rows = std::make_shared<lfg::Plan>();
+    const std::vector<CDim> T1{{nl, 1, 1}}, V1{{total / nl, nl, nl}};
+    lfg_status s = build_separable(*rows, false, T1, V1, {}, 0, 0, 1, precision, flags);
+    if (s != LFG_OK) return fail_free(s);
+    p.steps.push_back({lfg::PackStep::kPlan, {}, rows, 3, 2});
+    p.flops += rows->flops;
+    p.steps.push_back({lfg::PackStep::kScatter, pack_desc(lfg::kPackReal, ns, rst, rRe, -1, 0, total),
+                       nullptr, 2, 1});
+  }
+  return wrap_plan(p, out);
 }
 
 }  // namespace
@@ -483,45 +893,53 @@ lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precisi
   };
   // offsets and strides count real scalars of the plan's precision (doubles or floats)
   if (precision != LFG_F64 && precision != LFG_F32) return fail(LFG_ERR_INVALID, "bad precision");
+  // all dimensions, in real scalars (any sign of stride)
+  std::vector<SDim> ST, SV;
+  for (int64_t i = 0; i < rank + vrank; ++i) {
+    int64_t n, is, os;
+    dim(i, &n, &is, &os);
+    if (n < 0) return fail(LFG_ERR_INVALID, "negative dimension");
+    if (i < rank && n < 1) return fail(LFG_ERR_UNSUPPORTED, "transform dimension must be >= 1");
+    if (i < rank && n > ((int64_t)1 << 24)) return fail(LFG_ERR_UNSUPPORTED, "transform sizes above 2^24");
+    (i < rank ? ST : SV).push_back(SDim{n, is, os});
+  }
   if (kind == 1) {
     // rdft2 (Core/Problem.lean:222-236): r2c when sign < 0 (real input), else c2r; the last
-    // dimension is halved on the complex side.  Executed: rank 1 or 2, vector rank <= 1, unit
-    // stride along the last axis on both sides, interleaved complex side.
-    if (rank < 1 || rank > 2 || vrank > 1)
-      return fail(LFG_ERR_UNSUPPORTED, "rdft2: rank 1-2 and vector rank <= 1 are executed");
+    // dimension is halved on the complex side.  The fused kernels take rank 1 or 2, vector
+    // rank <= 1, unit stride along the last axis on both sides, an interleaved complex side and
+    // an even 13-smooth size; everything else goes through dense buffers and complex transforms.
+    if (rank < 1) return fail(LFG_ERR_UNSUPPORTED, "rdft2 needs rank >= 1");
     const bool r2c = sign < 0;
     const int64_t rRe = r2c ? inRe : outRe;
     const int64_t cRe = r2c ? outRe : inRe, cIm = r2c ? outIm : inIm;
-    if (cIm != cRe + 1 || (cRe & 1) || rRe < 0 || cRe < 0)
-      return fail(LFG_ERR_UNSUPPORTED, "rdft2: the complex side must be interleaved");
+    const SDim last = ST[rank - 1];
+    const int64_t rstl = r2c ? last.is : last.os, cstl = r2c ? last.os : last.is;
+    bool native = rank <= 2 && vrank <= 1 && cIm == cRe + 1 && !(cRe & 1) && rRe >= 0 && cRe >= 0 &&
+                  (rRe & 1) == 0 && rstl == 1 && cstl == 2 && last.n >= 2 && !(last.n & 1) &&
+                  smooth13(last.n) && (rank == 1 || smooth13(ST[0].n));
     lfg::RealLayout L;
-    int64_t nl, isl, osl;
-    dim(rank - 1, &nl, &isl, &osl);
-    const int64_t rstl = r2c ? isl : osl, cstl = r2c ? osl : isl;
-    if (rstl != 1 || cstl != 2)
-      return fail(LFG_ERR_UNSUPPORTED, "rdft2: unit stride along the last axis is required");
-    L.n = nl;
-    if (rank == 2) {
-      int64_t n0, is0, os0;
-      dim(0, &n0, &is0, &os0);
-      L.n0 = n0;
-      L.r_rdist = r2c ? is0 : os0;
-      const int64_t cr = r2c ? os0 : is0;
-      if (cr & 1) return fail(LFG_ERR_UNSUPPORTED, "rdft2: complex row pitch must be whole elements");
+    L.n = last.n;
+    if (native && rank == 2) {
+      L.n0 = ST[0].n;
+      L.r_rdist = r2c ? ST[0].is : ST[0].os;
+      const int64_t cr = r2c ? ST[0].os : ST[0].is;
       L.c_rdist = cr / 2;
+      native = !(cr & 1) && L.r_rdist > 0 && cr > 0 && (L.r_rdist & 1) == 0;
     }
     int64_t vn = 1, vis = 0, vos = 0;
-    if (vrank == 1) dim(rank, &vn, &vis, &vos);
-    if (vn < 0) return fail(LFG_ERR_INVALID, "negative vector dimension");
+    if (vrank == 1) {
+      vn = SV[0].n;
+      vis = SV[0].is;
+      vos = SV[0].os;
+    }
+    const int64_t cb = r2c ? vos : vis;
     L.howmany = vn;
     L.r_bdist = r2c ? vis : vos;
-    const int64_t cb = r2c ? vos : vis;
-    if (cb & 1) return fail(LFG_ERR_UNSUPPORTED, "rdft2: complex vector pitch must be whole elements");
     L.c_bdist = cb / 2;
+    native = native && !(cb & 1) && (vn <= 1 || (L.r_bdist > 0 && cb > 0 && (L.r_bdist & 1) == 0));
+    if (!native) return plan_rdft2_packed(r2c, ST, SV, rRe, cRe, cIm, precision, flags, out);
     L.r_off = rRe;
     L.c_off = cRe / 2;
-    if (L.n < 2 || !smooth13(L.n) || !smooth13(L.n0))
-      return fail(LFG_ERR_UNSUPPORTED, "rdft2: sizes must be 13-smooth");
     lfg::Plan p;
     p.kind = r2c ? lfg::Kind::R2C : lfg::Kind::C2R;
     p.precision = precision;
@@ -553,27 +971,20 @@ lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precisi
     return plan_separable(true, T, V, kinds, inRe, outRe, sign, precision, flags, out);
   }
   if (kind != 0) return fail(LFG_ERR_INVALID, "kind must be 0, 1 or 2");
-  for (int64_t d = 0; d < rank; ++d) {
-    int64_t n, is, os;
-    dim(d, &n, &is, &os);
-    if (n < 1) return fail(LFG_ERR_UNSUPPORTED, "transform dimension must be >= 1");
-  }
   if (rank < 1) return fail(LFG_ERR_UNSUPPORTED, "rank-0 problems (copies) are not executed");
-  // interleaved complex data: imaginary part one double after the real part, even strides
-  if (inIm != inRe + 1 || outIm != outRe + 1 || inRe < 0 || outRe < 0 || (inRe & 1) || (outRe & 1))
-    return fail(LFG_ERR_UNSUPPORTED, "only interleaved, complex-aligned layouts are executed");
+  // the kernels take interleaved complex data (imaginary part one scalar after the real part)
+  // at positive strides of whole complex elements; other layouts (split arrays, strides of
+  // either sign) go through dense buffers
+  bool interleaved = inIm == inRe + 1 && outIm == outRe + 1 && inRe >= 0 && outRe >= 0 &&
+                     !(inRe & 1) && !(outRe & 1);
+  for (const auto* Lst : {&ST, &SV})
+    for (const SDim& d : *Lst)
+      if (d.n > 1 && ((d.is & 1) || (d.os & 1) || d.is <= 0 || d.os <= 0)) interleaved = false;
+  if (!interleaved) return plan_c2c_packed(ST, SV, inRe, inIm, outRe, outIm, sign, precision, flags, out);
   if (rank > 1 || vrank > 1) {
     std::vector<CDim> T, V;
-    for (int64_t i = 0; i < rank + vrank; ++i) {
-      int64_t n, is, os;
-      dim(i, &n, &is, &os);
-      if (n < 0) return fail(LFG_ERR_INVALID, "negative dimension");
-      if (n > 1 && ((is & 1) || (os & 1) || is <= 0 || os <= 0))
-        return fail(LFG_ERR_UNSUPPORTED, "strides must be positive multiples of a complex element");
-      if (i < rank && (n > ((int64_t)1 << 24) || (n > 1 && !smooth13(n))))
-        return fail(LFG_ERR_UNSUPPORTED, "transform sizes must be 13-smooth and at most 2^24");
-      (i < rank ? T : V).push_back(CDim{n, is / 2, os / 2});
-    }
+    for (const SDim& d : ST) T.push_back(CDim{d.n, d.is / 2, d.os / 2});
+    for (const SDim& d : SV) V.push_back(CDim{d.n, d.is / 2, d.os / 2});
     return plan_separable(false, T, V, {}, inRe / 2, outRe / 2, sign, precision, flags, out);
   }
   int64_t n, is, os;
@@ -581,10 +992,9 @@ lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precisi
   int64_t vn = 1, vis = 0, vos = 0;
   if (vrank == 1) dim(1, &vn, &vis, &vos);
   if (vn < 0) return fail(LFG_ERR_INVALID, "negative vector dimension");
-  if ((is & 1) || (os & 1) || (vis & 1) || (vos & 1) || is <= 0 || os <= 0 || vis < 0 || vos < 0)
-    return fail(LFG_ERR_UNSUPPORTED, "strides must be positive multiples of a complex element");
-  if (n < 2 || n > ((int64_t)1 << 24) || !smooth13(n))
-    return fail(LFG_ERR_UNSUPPORTED, "size must be 13-smooth in 2..2^24");
+  if (vis < 0 || vos < 0 || (vis & 1) || (vos & 1))
+    return plan_c2c_packed(ST, SV, inRe, inIm, outRe, outIm, sign, precision, flags, out);
+  if (n < 2) return fail(LFG_ERR_UNSUPPORTED, "a transform of one point is a copy");
   lfg::Plan p;
   p.kind = lfg::Kind::C2C;
   p.precision = precision;
@@ -659,7 +1069,13 @@ lfg_status lfg_set_scale(lfg_plan* plan, double scale) {
   if (!std::isfinite(scale)) return fail(LFG_ERR_INVALID, "scale must be finite");
   lfg::Plan& p = plan->p;
   if (p.kind != lfg::Kind::C2C) return fail(LFG_ERR_UNSUPPORTED, "scaling applies to complex plans");
-  if (!p.stages.empty()) {
+  lfg::Plan* target = p.stages.empty() ? &p : p.stages.back().plan.get();
+  if (target->generic) {
+    target->gen.scale = scale;
+  } else if (target->chirp_bwd) {
+    lfg::Plan& b = *target->chirp_bwd;
+    if (b.ngroups >= 1) b.groups[b.ngroups - 1].scale = scale / (double)target->chirp.L;
+  } else if (!p.stages.empty()) {
     lfg::Plan& last = *p.stages.back().plan;
     if (last.ngroups >= 1) last.groups[last.ngroups - 1].scale = scale;
   } else if (p.ngroups >= 1) {

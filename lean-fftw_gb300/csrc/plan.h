@@ -8,6 +8,9 @@
 #include <string>
 #include <vector>
 
+#include "chirp.h"
+#include "generic.h"
+#include "pack.h"
 #include "r2r.h"
 #include "real.h"
 #include "stockham.h"
@@ -25,6 +28,16 @@ struct Side {
 };
 
 struct Plan;
+
+// One step of a plan that runs through dense buffers: gather (strided -> dense), scatter
+// (dense -> strided) or a whole inner plan.  Buffers: 0 the input, 1 the output, 2 and 3 the
+// plan's two dense buffers.
+struct PackStep {
+  enum Op { kGather, kScatter, kPlan } op;
+  PackDesc pd{};
+  std::shared_ptr<Plan> plan;
+  int src = 0, dst = 0;
+};
 
 // One axis of a multi-axis complex plan: a 1-D plan along the axis over the other dimensions,
 // launched once per entry of `loops` (input and output element offsets of batch dimensions
@@ -89,6 +102,22 @@ struct Plan {
   R2RDesc r2r{};
   std::shared_ptr<Plan> r2r_dft;
   void* d_r2r_buf = nullptr;
+  // complex sizes with a prime factor above 13 (Bluestein): forward and backward transforms
+  // of the convolution length L over all lines, two lines x L buffers, chirp and filter
+  ChirpDesc chirp{};
+  std::shared_ptr<Plan> chirp_fwd, chirp_bwd;
+  void* d_chirp_buf = nullptr;
+  void* d_chirp_tab = nullptr;
+  // small sizes with a prime factor above 13: the generic engine's transform, one CTA a line
+  bool generic = false;
+  GenericDesc gen{};
+  void* d_gen_tab = nullptr;
+  // problems the kernels do not take directly (split real/imaginary arrays, strides of either
+  // sign, odd, non-smooth or rank >= 3 real transforms) run as a list of steps through two
+  // dense complex buffers of pack_elems elements each
+  std::vector<PackStep> steps;
+  void* d_pack_buf = nullptr;
+  int64_t pack_elems = 0;
 };
 
 // Geometry of a real transform: vector count `howmany`, rank-2 size n0 x n (rank 1: n0 = 1).

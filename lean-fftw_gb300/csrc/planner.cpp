@@ -114,6 +114,20 @@ void free_plan_memory(Plan& p) {
   if (p.d_col_twiddles) cudaFree(p.d_col_twiddles);
   if (p.d_status) cudaFree(p.d_status);
   if (p.d_r2r_buf) cudaFree(p.d_r2r_buf);
+  if (p.d_gen_tab) cudaFree(p.d_gen_tab);
+  p.d_gen_tab = nullptr;
+  if (p.d_pack_buf) cudaFree(p.d_pack_buf);
+  p.d_pack_buf = nullptr;
+  for (PackStep& st : p.steps)
+    if (st.plan) free_plan_memory(*st.plan);
+  p.steps.clear();
+  if (p.d_chirp_buf) cudaFree(p.d_chirp_buf);
+  if (p.d_chirp_tab) cudaFree(p.d_chirp_tab);
+  if (p.chirp_fwd) free_plan_memory(*p.chirp_fwd);
+  if (p.chirp_bwd) free_plan_memory(*p.chirp_bwd);
+  p.chirp_fwd.reset();
+  p.chirp_bwd.reset();
+  p.d_chirp_buf = p.d_chirp_tab = nullptr;
   if (p.r2r_dft) free_plan_memory(*p.r2r_dft);
   p.r2r_dft.reset();
   p.d_r2r_buf = nullptr;
@@ -531,6 +545,38 @@ static cudaError_t ensure_scratch(const Plan& p) {
 cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream,
                          bool force_scratch) {
   if (p.empty) return cudaSuccess;
+  if (p.generic) {
+    const size_t ces = p.precision == 0 ? 16 : 8;
+    return launch_generic(p.gen, p.precision, p.fwd, static_cast<const char*>(in) + p.in.offset * (int64_t)ces,
+                          static_cast<char*>(out) + p.out.offset * (int64_t)ces, stream);
+  }
+  if (!p.steps.empty()) {
+    const size_t ces = p.precision == 0 ? 16 : 8;
+    void* bufs[4] = {const_cast<void*>(in), out, p.d_pack_buf,
+                     static_cast<char*>(p.d_pack_buf) + (size_t)p.pack_elems * ces};
+    for (const PackStep& st : p.steps) {
+      cudaError_t e;
+      if (st.op == PackStep::kGather) e = launch_pack(st.pd, p.precision, bufs[st.src], bufs[st.dst], stream);
+      else if (st.op == PackStep::kScatter) e = launch_unpack(st.pd, p.precision, bufs[st.src], bufs[st.dst], stream);
+      else e = execute_plan(*st.plan, bufs[st.src], bufs[st.dst], stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  if (p.chirp_fwd) {
+    // Bluestein: chirp and pad -> forward L -> filter -> backward L (scaled 1/L) -> chirp
+    const size_t ces = p.precision == 0 ? 16 : 8;
+    char* A = static_cast<char*>(p.d_chirp_buf);
+    char* B = A + (size_t)p.chirp.lines * (size_t)p.chirp.L * ces;
+    const char* ib = static_cast<const char*>(in) + p.in.offset * (int64_t)ces;
+    char* ob = static_cast<char*>(out) + p.out.offset * (int64_t)ces;
+    cudaError_t e = launch_chirp_pre(p.chirp, p.precision, ib, A, stream);
+    if (e == cudaSuccess) e = execute_plan(*p.chirp_fwd, A, B, stream);
+    if (e == cudaSuccess) e = launch_chirp_mul(p.chirp, p.precision, B, stream);
+    if (e == cudaSuccess) e = execute_plan(*p.chirp_bwd, B, A, stream);
+    if (e == cudaSuccess) e = launch_chirp_post(p.chirp, p.precision, A, ob, stream);
+    return e;
+  }
   if (p.kind == Kind::R2R && p.stages.empty()) {
     // embedding -> complex DFT of the embedding size -> extraction
     const size_t ces = p.precision == 0 ? 16 : 8;

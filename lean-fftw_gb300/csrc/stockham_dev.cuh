@@ -28,6 +28,8 @@ struct Prec<double> {
   using Bfly = BflyD<F, R, W>;
   static __device__ __forceinline__ C mk(double a, double b) { return make_double2(a, b); }
   static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
   static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
 };
 
@@ -38,6 +40,8 @@ struct Prec<float> {
   using Bfly = BflyF<F, R, W>;
   static __device__ __forceinline__ C mk(float a, float b) { return make_float2(a, b); }
   static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
   static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 };
 

@@ -50,17 +50,17 @@ def test_plan_without_gpu_fails_loudly():
 
 
 def test_unsupported_sizes_rejected_before_device_use():
-    # prime factor 17: lean-fftw's fast engine rejects it too (bench-leanfftw.c:253-268)
-    with pytest.raises(lfg.Unsupported):
-        lfg.plan_1d(17)
+    # sizes above 2^24, an explicit radix sequence for a size with a prime factor above 13
+    # (the fast engine's codelets stop at 13), REDFT00 of one point (undefined, as in the
+    # reference) and odd-length real transforms are refused before any device use
     with pytest.raises(lfg.Unsupported):
         lfg.plan_1d(1 << 25)
-    # r2r whose embedding size has a prime factor above 13 (REDFT00 of 18: a DFT of 34), and
-    # REDFT00 of one point (undefined, as in the reference), are refused before any device use
     with pytest.raises(lfg.Unsupported):
-        lfg.plan_spec([2, -1, 1, 0, 0, 0, 0, 0, 18, 1, 1, 3])
+        lfg.plan_1d(17, radices=[17])
     with pytest.raises(lfg.Unsupported):
         lfg.plan_r2r(1, "redft00")
+    with pytest.raises(lfg.Unsupported):
+        lfg.plan_r2c(15)
 
 
 def test_invalid_arguments():

@@ -64,8 +64,8 @@ GPU = torch.cuda.is_available()
 @pytest.mark.gpu
 @pytest.mark.skipif(not GPU, reason="no GPU")
 @pytest.mark.parametrize("prob,ok", [("ocf1024", True), ("ibf360*5", True), ("orf12x60", True),
-                                     ("ocf64x64", True), ("ocf17", False), ("ocf19x4", False),
-                                     ("orf15", False)])
+                                     ("ocf64x64", True), ("ocf17", True), ("ocf19x4", True),
+                                     ("orf15", True), ("ok1e00", False), ("ocf1", False)])
 def test_can_do(prob, ok):
     assert _run("--can-do", prob)[1] == ("#t" if ok else "#f")
 
