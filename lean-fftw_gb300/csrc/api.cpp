@@ -158,30 +158,20 @@ lfg_status build_generic_device(lfg::Plan& p) {
 // Device part of a 1-D complex plan: kernels set up, autotuning, groups and tables.
 lfg_status build_c2c_device(lfg::Plan& p) {
   if (!smooth13(p.n)) {
+    // binary64: the reference's own algorithm where its direct sums stay cheap; binary32 (no
+    // bit pattern to reproduce): Bluestein, whose error does not grow with the prime factors
     const std::vector<int> fs = prime_factors(p.n);
-    if (p.n <= lfg::kGenericMaxN && fs.back() <= 1024) return build_generic_device(p);
+    if (p.precision == 0 && p.n <= lfg::kGenericMaxN && fs.back() <= 1024)
+      return build_generic_device(p);
     return build_chirp_device(p);
   }
   // binary64 is bound by the FP64 pipe: two groups of small tiles (more CTAs per SM) beat one
   // group with a CTA-sized tile above 2048 points; binary32 is bound by HBM: as few groups as fit
-  const bool user_split = p.single_max > 0 || p.tile > 0;
   if (p.single_max == 0 && p.precision == 0) p.single_max = single_max_default();
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   p.device = dev;
-  // a small batch leaves most SMs idle with one CTA per tile of whole transforms, and one
-  // SM's FP64 pipe needs ~8 us for a 1024-point transform: split the transform into two
-  // balanced pass groups of one sub-problem per CTA instead, so that it spreads over
-  // N/P + P CTAs (lower latency; same operations, same result bits)
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t c1 = std::max<int64_t>(1, tile_target() / std::max<int64_t>(p.n, 1));
-  const int64_t tiles1 = (p.howmany * p.howmany2 + c1 - 1) / c1;
-  if (!user_split && !p.measure && p.n >= 256 && 4 * tiles1 < sms) {
-    p.single_max = p.n - 1;     // forces the most balanced two-group split
-    p.tile = 1;                 // one sub-problem per CTA
-  }
   if (!p.empty) {
     e = p.precision == 0 ? lfg::prepare_group_kernels_f64() : lfg::prepare_group_kernels_f32();
     if (e != cudaSuccess) return cuda_fail(e, "kernel set-up");

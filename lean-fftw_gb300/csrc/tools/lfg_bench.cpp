@@ -132,7 +132,7 @@ Problem parse(const std::string& s) {
   }
   if (rest.empty()) p.err = "no transform dimensions";
   else if (parse_dims(rest, &p.sz, &p.err) && !vec.empty()) parse_dims(vec, &p.vec, &p.err);
-  if (p.err.empty() && p.split) p.err = "split real/imaginary arrays are not executed";
+  if (p.err.empty() && p.split && p.kind == 'k') p.err = "r2r problems have no split arrays";
   // an r2r dimension without a kind suffix is R2HC forward, HC2R backward; other problems
   // take no kind suffixes
   for (Dim& d : p.sz) {
@@ -165,6 +165,11 @@ struct Layout {
   std::vector<Dim> sz, vec;
   bool in_real = false, out_real = false;
   int64_t in_lo = 0, in_hi = 0, out_lo = 0, out_hi = 0;   // element offset ranges
+  // element o of a side (offset relative to the low end of its span) has its real part at
+  // double re + mult * o and its imaginary part at im + mult * o (interleaved: im = re + 1,
+  // mult 2; split arrays: the imaginary array follows the real one, mult 1)
+  int64_t in_re = 0, in_im = 0, out_re = 0, out_im = 0, in_mult = 2, out_mult = 2;
+  int64_t in_len = 0, out_len = 0;   // doubles of each buffer
   std::vector<double> spec;
 };
 
@@ -209,15 +214,32 @@ Layout layout(const Problem& p) {
   span(all, false, (real && !L.in_real) ? r - 1 : -1, &L.in_lo, &L.in_hi);
   span(all, true, (real && !L.out_real) ? r - 1 : -1, &L.out_lo, &L.out_hi);
   // spec: strides and offsets in doubles; buffers start at the low end of each span
-  const double im = L.in_real ? 1 : 2, om = L.out_real ? 1 : 2;
-  int64_t in0 = -L.in_lo, out0 = -L.out_lo;
-  if (p.inplace) {
-    const int64_t lo = std::min(L.in_lo * (int64_t)im, L.out_lo * (int64_t)om);
-    in0 = -lo / (int64_t)im;
-    out0 = -lo / (int64_t)om;
-  }
+  const int64_t in_span = L.in_hi - L.in_lo + 1, out_span = L.out_hi - L.out_lo + 1;
+  const int64_t span_both = std::max(in_span, out_span);
+  auto side = [&](bool is_real, int64_t lo, int64_t span, int64_t* re, int64_t* imb, int64_t* mult,
+                  int64_t* len) {
+    if (is_real) {
+      *mult = 1;
+      *re = -lo;
+      *imb = *re;
+      *len = span;
+    } else if (p.split) {
+      *mult = 1;
+      *re = -lo;
+      *imb = *re + (p.inplace ? span_both : span);
+      *len = 2 * (p.inplace ? span_both : span);
+    } else {
+      *mult = 2;
+      *re = -2 * lo;
+      *imb = *re + 1;
+      *len = 2 * span;
+    }
+  };
+  side(L.in_real, L.in_lo, in_span, &L.in_re, &L.in_im, &L.in_mult, &L.in_len);
+  side(L.out_real, L.out_lo, out_span, &L.out_re, &L.out_im, &L.out_mult, &L.out_len);
+  const double im = (double)L.in_mult, om = (double)L.out_mult;
   L.spec = {r2r ? 2.0 : real ? 1.0 : 0.0, (double)p.sign, (double)r, (double)p.vec.size(),
-            in0 * im, in0 * im + (r2r ? 0 : 1), out0 * om, out0 * om + (r2r ? 0 : 1)};
+            (double)L.in_re, (double)L.in_im, (double)L.out_re, (double)L.out_im};
   for (const Dim& d : L.sz) {
     L.spec.push_back((double)d.n);
     L.spec.push_back(d.is * im);
@@ -235,11 +257,9 @@ Layout layout(const Problem& p) {
 
 // doubles each side's buffer holds
 int64_t in_doubles(const Layout& L, bool inplace) {
-  const int64_t a = (L.in_hi - L.in_lo + 1) * (L.in_real ? 1 : 2);
-  const int64_t b = (L.out_hi - L.out_lo + 1) * (L.out_real ? 1 : 2);
-  return inplace ? std::max(a, b) + 2 : a;
+  return inplace ? std::max(L.in_len, L.out_len) + 2 : L.in_len;
 }
-int64_t out_doubles(const Layout& L) { return (L.out_hi - L.out_lo + 1) * (L.out_real ? 1 : 2); }
+int64_t out_doubles(const Layout& L) { return L.out_len; }
 
 struct Runner {
   Problem p;
@@ -305,10 +325,7 @@ struct Runner {
       off += (q % n) * (out_side ? L.vec[d].os : L.vec[d].is);
       q /= n;
     }
-    const double* spec = L.spec.data();
-    const int64_t base = (int64_t)(out_side ? spec[6] : spec[4]) /
-                         ((out_side ? L.out_real : L.in_real) ? 1 : 2);
-    return base + off;
+    return off - (out_side ? L.out_lo : L.in_lo);
   }
   // run on a logical input (complex values; real sides use the real parts)
   std::vector<cplx> run(const std::vector<cplx>& x) {
@@ -316,8 +333,8 @@ struct Runner {
     std::memset(hin, 0, nin * 8);
     for (int64_t q = 0; q < (int64_t)x.size(); ++q) {
       const int64_t o = offset(q, false, ih);
-      if (L.in_real) hin[o] = x[q].real();
-      else { hin[2 * o] = x[q].real(); hin[2 * o + 1] = x[q].imag(); }
+      hin[L.in_re + L.in_mult * o] = x[q].real();
+      if (!L.in_real) hin[L.in_im + L.in_mult * o] = x[q].imag();
     }
     if (device) {
       cudaMemcpy(din, hin, nin * 8, cudaMemcpyHostToDevice);
@@ -329,7 +346,8 @@ struct Runner {
     std::vector<cplx> y(count(true, oh));
     for (int64_t q = 0; q < (int64_t)y.size(); ++q) {
       const int64_t o = offset(q, true, oh);
-      y[q] = L.out_real ? cplx(hout[o], 0.0) : cplx(hout[2 * o], hout[2 * o + 1]);
+      y[q] = L.out_real ? cplx(hout[L.out_re + o], 0.0)
+                        : cplx(hout[L.out_re + L.out_mult * o], hout[L.out_im + L.out_mult * o]);
     }
     return y;
   }

@@ -46,7 +46,7 @@ def test_negative_strides_c2c():
     # element j at double offset 2(n-1-j): re at 2(n-1) - 2j, im one after
     spec = [0, -1, 1, 0, 2 * (n - 1), 2 * (n - 1) + 1, 2 * (n - 1), 2 * (n - 1) + 1, n, -2, -2]
     plan, o = _exec_spec(spec, buf, 2 * n)
-    y = o.view(np.complex128)[::-1]
+    y = np.ascontiguousarray(o.view(np.complex128)[::-1])
     ref = O.ref_transform(True, n, plan.radices, x[::-1].copy()[None])[0]
     assert np.array_equal(y.view(np.uint64), ref.view(np.uint64))
 
