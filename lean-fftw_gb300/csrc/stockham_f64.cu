@@ -15,6 +15,7 @@
 
 #include <algorithm>
 
+#include "ragged_parts.h"
 #include "stockham_dev.cuh"
 
 namespace lfg {
@@ -31,72 +32,6 @@ group_kernel_f64(const GroupDesc g, const double2* in, double2* out) {
   process_tile_f64<FWD>(g, StridedLines{g.in_line, g.out_line}, s0, C, in, out, smem_f64);
 }
 
-// Persistent kernel over a ragged batch: each CTA takes work items from a queue (an atomic
-// ticket counter, zeroed before the launch) until it is empty.  An item is a tile of up to
-// C transforms of one size (one group), or one whole transform of a two-group size, whose
-// first group writes its intermediate to the output and whose second group then works on
-// the output in place; the barrier between them orders the global-memory traffic within
-// the CTA.  Items are sorted by decreasing cost, so the largest start first.
-// One fixed base per side (a single line): the two-group items that stage their
-// intermediate in a CTA-private scratch slab instead of the output.
-struct FixedBases {
-  int64_t in_base, out_base;
-  __device__ int64_t in(int64_t) const { return in_base; }
-  __device__ int64_t out(int64_t) const { return out_base; }
-  __device__ int64_t pitch(bool) const { return -1; }
-};
-
-template <bool FWD, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB)
-ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __restrict__ items,
-                  int nitems, const int64_t* __restrict__ in_off,
-                  const int64_t* __restrict__ out_off, const double2* in, double2* out,
-                  unsigned int* counter, double2* scratch, int64_t slab) {
-  extern __shared__ double2 smem_f64[];
-  __shared__ int s_item;
-  for (;;) {
-    if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
-    __syncthreads();
-    const int it = s_item;
-    if (it >= nitems) break;
-    const RaggedItem w = items[it];
-    const RaggedClass& rc = classes[w.cls];
-    const ListedLines lines{in_off, out_off, w.first};
-    if (rc.ngroups == 1) {
-      process_tile_f64<FWD>(rc.g[0], lines, 0, w.count, in, out, smem_f64);
-    } else if (scratch) {
-      // intermediate in this CTA's slab of device memory (the output may be host memory)
-      const GroupDesc& g1 = rc.g[0];
-      const GroupDesc& g2 = rc.g[1];
-      double2* mine = scratch + (int64_t)blockIdx.x * slab;
-      const FixedBases first{__ldg(in_off + w.first), 0};
-      const FixedBases second{0, __ldg(out_off + w.first)};
-      for (int64_t s0 = 0; s0 < g1.nsub; s0 += g1.C) {
-        process_tile_f64<FWD>(g1, first, s0, (int)min((int64_t)g1.C, g1.nsub - s0), in, mine, smem_f64);
-        __syncthreads();
-      }
-      for (int64_t s0 = 0; s0 < g2.nsub; s0 += g2.C) {
-        process_tile_f64<FWD>(g2, second, s0, (int)min((int64_t)g2.C, g2.nsub - s0), mine, out, smem_f64);
-        __syncthreads();
-      }
-    } else {
-      const GroupDesc& g1 = rc.g[0];
-      const GroupDesc& g2 = rc.g[1];
-      for (int64_t s0 = 0; s0 < g1.nsub; s0 += g1.C) {
-        process_tile_f64<FWD>(g1, lines, s0, (int)min((int64_t)g1.C, g1.nsub - s0), in, out, smem_f64);
-        __syncthreads();
-      }
-      // the second group reads the first group's result from the output
-      const ListedLines inner{out_off, out_off, w.first};
-      for (int64_t s0 = 0; s0 < g2.nsub; s0 += g2.C) {
-        process_tile_f64<FWD>(g2, inner, s0, (int)min((int64_t)g2.C, g2.nsub - s0), out, out, smem_f64);
-        __syncthreads();
-      }
-    }
-    __syncthreads();   // every thread has read s_item before it is overwritten
-  }
-}
-
 }  // namespace
 
 size_t group_smem_bytes_f64(const GroupDesc& g) {
@@ -109,37 +44,27 @@ size_t ragged_smem_bytes_f64(const RaggedClass& c) {
   return m;
 }
 
-// Block shapes of the persistent kernel the autotuner chooses from: (threads, minimum
-// resident CTAs per SM, which caps the registers per thread).
-using RaggedFn = void (*)(const RaggedClass*, const RaggedItem*, int, const int64_t*,
-                          const int64_t*, const double2*, double2*, unsigned int*, double2*,
-                          int64_t);
-
-template <bool FWD>
-RaggedFn ragged_fn(int variant) {
-  switch (variant) {
-    case 1: return ragged_kernel_f64<FWD, 256, 1>;
-    case 2: return ragged_kernel_f64<FWD, 128, 2>;
-    case 3: return ragged_kernel_f64<FWD, 128, 3>;
-    case 4: return ragged_kernel_f64<FWD, 512, 1>;
-    default: return ragged_kernel_f64<FWD, 256, 2>;
+static RaggedFn ragged_fn(bool fwd, int variant) {
+  switch (variant * 2 + (fwd ? 1 : 0)) {
+    case 1: return ragged_part_fn<1>();
+    case 2: return ragged_part_fn<2>();
+    case 3: return ragged_part_fn<3>();
+    case 4: return ragged_part_fn<4>();
+    case 5: return ragged_part_fn<5>();
+    case 6: return ragged_part_fn<6>();
+    case 7: return ragged_part_fn<7>();
+    case 8: return ragged_part_fn<8>();
+    case 9: return ragged_part_fn<9>();
+    default: return ragged_part_fn<0>();
   }
 }
 
-int ragged_variant_threads(int variant) {
-  switch (variant) {
-    case 1: return 256;
-    case 2: return 128;
-    case 3: return 128;
-    case 4: return 512;
-    default: return 256;
-  }
-}
+int ragged_variant_threads(int variant) { return ragged_shape_threads(variant); }
 
 cudaError_t launch_ragged_f64(const RaggedLaunch& r, bool fwd, const void* in, void* out,
                               cudaStream_t stream, void* scratch, int64_t slab) {
   if (r.nitems <= 0) return cudaSuccess;
-  RaggedFn kern = fwd ? ragged_fn<true>(r.variant) : ragged_fn<false>(r.variant);
+  RaggedFn kern = ragged_fn(fwd, r.variant);
   kern<<<r.grid, ragged_variant_threads(r.variant), r.smem, stream>>>(
       r.classes, r.items, r.nitems, r.in_off, r.out_off, static_cast<const double2*>(in),
       static_cast<double2*>(out), r.counter, static_cast<double2*>(scratch), slab);
@@ -148,7 +73,7 @@ cudaError_t launch_ragged_f64(const RaggedLaunch& r, bool fwd, const void* in, v
 
 int ragged_blocks_per_sm_f64(size_t smem, int variant) {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ragged_fn<true>(variant),
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, ragged_fn(true, variant),
                                                     ragged_variant_threads(variant), smem) != cudaSuccess)
     return 1;
   return nb > 0 ? nb : 1;
@@ -171,8 +96,8 @@ cudaError_t prepare_group_kernels_f64() {
   if ((e = allow_max_smem(group_kernel_f64<true>)) != cudaSuccess) return e;
   if ((e = allow_max_smem(group_kernel_f64<false>)) != cudaSuccess) return e;
   for (int v = 0; v < kRaggedVariants; ++v) {
-    if ((e = allow_max_smem(ragged_fn<true>(v))) != cudaSuccess) return e;
-    if ((e = allow_max_smem(ragged_fn<false>(v))) != cudaSuccess) return e;
+    if ((e = allow_max_smem(ragged_fn(true, v))) != cudaSuccess) return e;
+    if ((e = allow_max_smem(ragged_fn(false, v))) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }

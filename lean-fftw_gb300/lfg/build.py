@@ -30,6 +30,9 @@ REPO = os.path.dirname(ROOT)
 
 GPU_RADICES = list(range(2, 17))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# sources compiled several times, once per -DLFG_PART value (large template instantiations
+# split over translation units so they compile in parallel)
+PARTS = {"ragged_f64.cu": 10}
 
 
 def nvcc() -> str:
@@ -86,7 +89,7 @@ def _digest(paths) -> str:
     return h.hexdigest()[:16]
 
 
-def compile_all(verbose: bool = False, jobs: int = 8) -> str:
+def compile_all(verbose: bool = False, jobs: int = 0) -> str:
     os.makedirs(BUILD, exist_ok=True)
     cu, cpp = _sources()
     headers = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".h", ".cuh"))]
@@ -98,11 +101,16 @@ def compile_all(verbose: bool = False, jobs: int = 8) -> str:
     objs = []
     for f in cu:
         src = os.path.join(CSRC, f)
-        obj = os.path.join(BUILD, f"{f}.{_digest([src])}.{common}.o")
-        cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-               "-Xptxas", "-v" if verbose else "-O3", *inc, "-c", src, "-o", obj]
-        jobs_list.append((obj, cmd))
-        objs.append(obj)
+        for part in range(PARTS.get(f, 0)) if f in PARTS else [None]:
+            tag = "" if part is None else f".p{part}"
+            obj = os.path.join(BUILD, f"{f}{tag}.{_digest([src])}.{common}.o")
+            cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                   "-Xptxas", "-v" if verbose else "-O3", *inc]
+            if part is not None:
+                cmd.append(f"-DLFG_PART={part}")
+            cmd += ["-c", src, "-o", obj]
+            jobs_list.append((obj, cmd))
+            objs.append(obj)
     for f in cpp:
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f"{f}.{_digest([src])}.{common}.o")
@@ -120,7 +128,9 @@ def compile_all(verbose: bool = False, jobs: int = 8) -> str:
             raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         return obj, r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
+    # longest compiles first, so the pool's tail is short
+    jobs_list.sort(key=lambda j: 0 if any(k in j[0] for k in ("ragged_f64", "stockham")) else 1)
+    with cf.ThreadPoolExecutor(max_workers=jobs or max(4, os.cpu_count() or 4)) as ex:
         for obj, log in ex.map(run, jobs_list):
             if verbose and log:
                 print(log)
