@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -54,6 +55,12 @@ int64_t single_max_default() {
     if (v >= 2) return v;
   }
   return 2048;
+}
+
+// The kernels move whole complex elements (binary64: 16 bytes, binary32: 8 bytes), real
+// lines included (read as pairs), so buffers must start on that boundary.
+bool element_aligned(const void* p, int precision) {
+  return ((uintptr_t)p & (precision == 0 ? 15u : 7u)) == 0;
 }
 
 // Device address of pinned (page-locked) host memory covering [p, p + bytes), or nullptr.
@@ -1007,6 +1014,8 @@ lfg_status lfg_execute(const lfg_plan* plan, const void* in, void* out, void* st
   if (!plan) return fail(LFG_ERR_INVALID, "null plan");
   if (plan->p.empty) return LFG_OK;
   if (!in || !out) return fail(LFG_ERR_INVALID, "null buffer");
+  if (!element_aligned(in, plan->p.precision) || !element_aligned(out, plan->p.precision))
+    return fail(LFG_ERR_INVALID, "buffers must be aligned to a complex element (16 bytes binary64, 8 bytes binary32)");
   cudaError_t e = lfg::execute_plan(plan->p, in, out, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "execute");
   return LFG_OK;
@@ -1023,7 +1032,8 @@ lfg_status lfg_execute_host(const lfg_plan* plan, const void* in, void* out) {
   {
     void* mi = mapped_device_ptr(in, ib);
     void* mo = in == out ? mi : mapped_device_ptr(out, ob);
-    if (mi && mo) {   // pinned host buffers: the kernels stream them over NVLink-C2C
+    if (mi && mo && element_aligned(mi, p.precision) && element_aligned(mo, p.precision)) {
+      // pinned host buffers: the kernels stream them over NVLink-C2C
       if ((e = lfg::execute_plan(p, mi, mo, 0, true)) != cudaSuccess) return cuda_fail(e, "execute");
       if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return cuda_fail(e, "execute");
       return LFG_OK;
@@ -1197,6 +1207,8 @@ lfg_status lfg_execute_ragged(const lfg_ragged* plan, const void* in, void* out,
   if (plan->r.empty) return LFG_OK;
   if (!in || !out) return fail(LFG_ERR_INVALID, "null buffer");
   if (in == out) return fail(LFG_ERR_UNSUPPORTED, "ragged batches run out of place");
+  if (!element_aligned(in, plan->r.precision) || !element_aligned(out, plan->r.precision))
+    return fail(LFG_ERR_INVALID, "buffers must be aligned to a complex element (16 bytes binary64, 8 bytes binary32)");
   cudaError_t e = lfg::execute_ragged(plan->r, in, out, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "execute ragged");
   return LFG_OK;
@@ -1213,7 +1225,8 @@ lfg_status lfg_execute_ragged_host(const lfg_ragged* plan, const void* in, void*
   {
     void* mi = mapped_device_ptr(in, ib);
     void* mo = mapped_device_ptr(out, ob);
-    if (mi && mo) {   // pinned host buffers: the kernel streams them over NVLink-C2C
+    if (mi && mo && element_aligned(mi, r.precision) && element_aligned(mo, r.precision)) {
+      // pinned host buffers: the kernel streams them over NVLink-C2C
       if ((e = lfg::execute_ragged_mapped(r, mi, mo, 0)) != cudaSuccess) return cuda_fail(e, "execute ragged");
       if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return cuda_fail(e, "execute ragged");
       return LFG_OK;

@@ -40,7 +40,18 @@ cudaError_t launch_tile_stream_f32(const GroupDesc& g, bool fwd, const void* in,
 // Persistent FP64 kernel over a ragged batch (one launch for all sizes), in kRaggedVariants
 // block shapes (threads x minimum CTAs per SM).
 constexpr int kRaggedVariants = 5;
-size_t ragged_smem_bytes_f64(const RaggedClass& c);
+// Shared memory: three tile buffers (a stage buffer and two work buffers) of `buf` complex
+// elements each.
+constexpr size_t ragged_smem_bytes_f64(int64_t buf) { return 3 * (size_t)buf * 16; }
+inline bool ragged_tile_fits(int64_t C, int64_t M) {
+  return ragged_smem_bytes_f64(tile_elems(C, (int)M)) <= kSmemBudget;
+}
+// Largest size a ragged batch runs as one pass group (one tile of one transform fits).
+inline int64_t ragged_max_single_group() {
+  int64_t n = (int64_t)(kSmemBudget / 48);
+  while (n > 1 && !ragged_tile_fits(1, n)) --n;
+  return n;
+}
 int ragged_variant_threads(int variant);
 int ragged_blocks_per_sm_f64(size_t smem, int variant);
 // scratch (optional): grid x slab complex elements of device memory; when given, two-group

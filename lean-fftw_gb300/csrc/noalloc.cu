@@ -18,6 +18,7 @@
 // clearing, but two calls whose executions overlap on the GPU race on it.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -92,6 +93,10 @@ extern "C" lfg_status lfg_execute_inplace_static(const lfg_plan* plan, void* dat
     return LFG_ERR_UNSUPPORTED;
   }
   if (p.empty) return LFG_OK;
+  if ((uintptr_t)data & (p.precision == 0 ? 15u : 7u)) {
+    lfg::set_last_error("buffer must be aligned to a complex element (16 bytes binary64, 8 bytes binary32)");
+    return LFG_ERR_INVALID;
+  }
   if (!p.stages.empty() || p.howmany2 > 1) {
     lfg::set_last_error("static-scratch execution takes 1-D plans with one batch dimension");
     return LFG_ERR_UNSUPPORTED;

@@ -86,7 +86,8 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
     // pass grouping: the per-size strategy splits at the shared-memory limit, the persistent
     // kernel at opt.single_max; the second group's tables are stored transposed
     split_c[c] = split_point(n, r.class_radices[c],
-                             r.per_size_mode ? max_single_group(prec) : opt.single_max);
+                             r.per_size_mode ? max_single_group(prec)
+                                             : std::min(opt.single_max, ragged_max_single_group()));
     if (split_c[c] < 0) return "size " + std::to_string(n) + " needs more than two pass groups";
     transpose_second_group(tables[c], r.class_radices[c], split_c[c], {});
     base[c] = total;
@@ -101,10 +102,11 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
   if (!r.d_twiddles) return err;
   const size_t scal = prec == 0 ? sizeof(double) : sizeof(float);
 
-  // groups and work items
+  // groups and work items; the persistent kernel holds three tile buffers of the largest
+  // tile (ragged_tile_fits)
   std::vector<RaggedItem> items;
   std::vector<double> item_cost;
-  size_t smem = 0;
+  int64_t buf = 0;
   for (int c = 0; c < ncls; ++c) {
     const int64_t n = r.class_n[c];
     const std::vector<int>& rs = r.class_radices[c];
@@ -118,7 +120,7 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
       GroupDesc& g = rc.g[0];
       fill_group(g, rs, tables[c], 0, (int)rs.size(), 1, opt.tile_target, prec, tw);
       int64_t cmax = std::max<int64_t>(1, opt.tile_target / n);
-      while (cmax > 1 && smem_bytes(cmax, n, prec) > kSmemBudget) --cmax;
+      while (cmax > 1 && !ragged_tile_fits(cmax, n)) --cmax;
       g.C = (int)std::min<int64_t>(cmax, r.class_count[c]);
       g.in_sub = g.out_sub = 0;
       g.in_elem = g.out_elem = 1;
@@ -153,7 +155,11 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
         item_cost.push_back(ops_one);
       }
     }
-    for (int gi = 0; gi < rc.ngroups; ++gi) smem = std::max(smem, smem_bytes(rc.g[gi].C, rc.g[gi].M, prec));
+    for (int gi = 0; gi < rc.ngroups; ++gi) {
+      GroupDesc& g = rc.g[gi];
+      while (g.C > 1 && !ragged_tile_fits(g.C, g.M)) --g.C;
+      buf = std::max<int64_t>(buf, tile_elems(g.C, g.M));
+    }
   }
   // largest items first
   std::vector<size_t> perm(items.size());
@@ -185,7 +191,9 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
   r.launch.in_off = static_cast<const int64_t*>(r.d_in_off);
   r.launch.out_off = static_cast<const int64_t*>(r.d_out_off);
   r.launch.counter = static_cast<unsigned*>(r.d_counter);
-  r.launch.smem = smem;
+  r.launch.buf = (int)buf;
+  r.launch.smem = ragged_smem_bytes_f64(buf);
+  const size_t smem = r.launch.smem;
   r.launch.variant = opt.variant;
   const int per_sm = prec == 0 ? ragged_blocks_per_sm_f64(smem, opt.variant) : 1;
   const int64_t want = (int64_t)prop.multiProcessorCount * per_sm;

@@ -11,7 +11,7 @@ namespace lfg {
 
 using RaggedFn = void (*)(const RaggedClass*, const RaggedItem*, int, const int64_t*,
                           const int64_t*, const double2*, double2*, unsigned int*, double2*,
-                          int64_t);
+                          int64_t, int);
 
 // Block shapes the autotuner chooses from: threads per CTA and the minimum resident CTAs per
 // SM (which caps the registers per thread).

@@ -141,7 +141,8 @@ struct RaggedLaunch {
   const int64_t* out_off;
   unsigned int* counter;
   unsigned grid;
-  size_t smem;
+  size_t smem;           // three tile buffers of `buf` complex elements
+  int buf;
   int variant;           // block shape of the persistent kernel (kernels.h)
 };
 

@@ -38,12 +38,6 @@ size_t group_smem_bytes_f64(const GroupDesc& g) {
   return 2 * (size_t)tile_elems(g.C, g.M) * sizeof(double2);
 }
 
-size_t ragged_smem_bytes_f64(const RaggedClass& c) {
-  size_t m = 0;
-  for (int i = 0; i < c.ngroups; ++i) m = std::max(m, group_smem_bytes_f64(c.g[i]));
-  return m;
-}
-
 static RaggedFn ragged_fn(bool fwd, int variant) {
   switch (variant * 2 + (fwd ? 1 : 0)) {
     case 1: return ragged_part_fn<1>();
@@ -67,7 +61,7 @@ cudaError_t launch_ragged_f64(const RaggedLaunch& r, bool fwd, const void* in, v
   RaggedFn kern = ragged_fn(fwd, r.variant);
   kern<<<r.grid, ragged_variant_threads(r.variant), r.smem, stream>>>(
       r.classes, r.items, r.nitems, r.in_off, r.out_off, static_cast<const double2*>(in),
-      static_cast<double2*>(out), r.counter, static_cast<double2*>(scratch), slab);
+      static_cast<double2*>(out), r.counter, static_cast<double2*>(scratch), slab, r.buf);
   return cudaGetLastError();
 }
 

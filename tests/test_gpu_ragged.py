@@ -104,3 +104,58 @@ def test_ragged_measured_plan_bitexact():
     plan.execute(xd, yd)
     torch.cuda.synchronize()
     assert not _check(plan, sizes, x, yd.cpu().numpy(), plan.in_offsets, plan.out_offsets)
+
+
+def test_ragged_pinned_host_entry():
+    """Pinned host buffers: the persistent kernel reads and writes host memory directly
+    (asynchronous tile copies from host memory, two-group intermediates in device slabs)."""
+    sizes = lfg.ragged_sizes(1024, seed=5)
+    sizes[:3] = [16384, 15015, 4096]          # two-group items next to one-group ones
+    plan = lfg.plan_ragged(sizes, -1)
+    total = int(sizes.sum())
+    x = O.uniform_complex((total,), seed=21)
+    hin = torch.from_numpy(x).pin_memory()
+    hout = torch.full((total,), SENT, dtype=torch.complex128).pin_memory()
+    for _ in range(2):
+        plan.execute_host(hin.numpy(), hout.numpy())
+    assert not _check(plan, sizes, x, hout.numpy(), plan.in_offsets, plan.out_offsets)
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("tile,single", [(2048, 2048), (4096, 4096), (1024, 1024)])
+def test_ragged_block_shapes(shape, tile, single):
+    """Every block shape of the persistent kernel, with the tile and single-group limits the
+    autotuner chooses from (three tile buffers must fit the shared memory)."""
+    sizes = lfg.ragged_sizes(384, seed=shape * 7 + tile // 1024)
+    sizes[:2] = [4096, 3000]
+    plan = lfg.plan_ragged(sizes, 1, block_shape=shape, tile_target=tile, single_max=single)
+    assert plan.info().smem_bytes <= 232448 - 1024
+    x = O.uniform_complex((int(sizes.sum()),), seed=shape)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(xd)
+    plan.execute(xd, yd)
+    torch.cuda.synchronize()
+    y = yd.cpu().numpy()
+    bad = []
+    for i, (a, o, n) in enumerate(zip(plan.in_offsets, plan.out_offsets, sizes)):
+        ref = O.ref_transform(False, int(n), plan.radices(int(n)), x[a: a + n])
+        if not np.array_equal(y[o: o + n].view(np.uint64), ref.view(np.uint64)):
+            bad.append(int(n))
+    assert not bad
+
+
+def test_ragged_rejects_misaligned_buffers():
+    """Buffers must start on a complex element: an 8-byte offset is refused before launch."""
+    import ctypes
+    from lfg._lib import LFG_ERR_INVALID
+    sizes = np.array([64, 12], dtype=np.int64)
+    plan = lfg.plan_ragged(sizes, -1)
+    buf = torch.zeros(200, dtype=torch.complex128, device="cuda")
+    p = buf.data_ptr()
+    st = lfg.lib().lfg_execute_ragged(plan._h, ctypes.c_void_p(p + 8), ctypes.c_void_p(p + 1600),
+                                      None)
+    assert st == LFG_ERR_INVALID
+    p1 = lfg.plan_1d(64, -1, 2)
+    st = lfg.lib().lfg_execute(p1._h, ctypes.c_void_p(p), ctypes.c_void_p(p + 2056), None)
+    assert st == LFG_ERR_INVALID
+    torch.cuda.synchronize()
