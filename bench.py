@@ -336,6 +336,9 @@ def main():
     ap.add_argument("--workload", default="ragged", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="lfg", choices=["lfg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--untuned", action="store_true",
+                    help="ragged: plan with the default schedule instead of autotuning it "
+                         "(profiling runs, where the tuner's candidate launches would be captured)")
     ap.add_argument("--batch", type=int, default=0,
                     help="override the batch of a c2c workload (smaller cases for profiling)")
     args = ap.parse_args()
@@ -368,7 +371,9 @@ def main():
     if wl["kind"] == "ragged":
         sizes = ragged_workload_sizes(wl)
         total = int(sizes.sum())
-        plan = lfg.plan_ragged(sizes, wl["sign"])
+        t_plan = time.perf_counter()
+        plan = lfg.plan_ragged(sizes, wl["sign"], measure=not args.untuned)   # autotuned
+        t_plan = time.perf_counter() - t_plan
         per_size = lfg.plan_ragged(sizes, wl["sign"], per_size=True)
         rinfo = plan.info()
         host = (rng.random((total, 2)) - 0.5).view(np.complex128).reshape(total)
@@ -380,7 +385,11 @@ def main():
         host_fn = lambda a, b: plan.execute_host(a, b)
         extra["config_extra"] = {"distinct_sizes": int(rinfo.classes), "points": total,
                                  "work_items": int(rinfo.items), "grid": int(rinfo.grid),
-                                 "smem_bytes": int(rinfo.smem_bytes)}
+                                 "smem_bytes": int(rinfo.smem_bytes),
+                                 "autotuned": {"block_shape": int(rinfo.block_shape),
+                                               "tile": int(rinfo.tile_target),
+                                               "single_group_max": int(rinfo.single_max),
+                                               "planning_s": round(t_plan, 2)}}
     elif wl["kind"] == "r2c2d":
         n0, n1, B = wl["n0"], wl["n1"], wl["batch"]
         prec = wl.get("precision", "f64")

@@ -198,6 +198,9 @@ typedef struct {
   int64_t in_bytes, out_bytes;
   int64_t points;       /* sum of the sizes                              */
   double flops;         /* binary64 instructions of the codelets         */
+  int64_t tile_target;  /* schedule in use (chosen by LFG_MEASURE, given by a tuning, or */
+  int64_t single_max;   /* the defaults): tile, single-group limit, block shape          */
+  int64_t block_shape;
 } lfg_ragged_info;
 
 lfg_status lfg_get_ragged_info(const lfg_ragged *plan, lfg_ragged_info *info);

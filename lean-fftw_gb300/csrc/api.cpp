@@ -1274,6 +1274,9 @@ lfg_status lfg_get_ragged_info(const lfg_ragged* plan, lfg_ragged_info* info) {
   info->out_bytes = r.out_span * es;
   for (int64_t n : r.sizes) info->points += n;
   info->flops = r.flops;
+  info->tile_target = r.options.tile_target;
+  info->single_max = std::min(r.options.single_max, lfg::ragged_max_single_group());
+  info->block_shape = r.options.variant;
   return LFG_OK;
 }
 

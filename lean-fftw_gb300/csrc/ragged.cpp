@@ -13,9 +13,11 @@
 #include "ragged.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <numeric>
+#include <thread>
 
 #include "generated/opcounts.h"
 #include "kernels.h"
@@ -82,7 +84,35 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
     r.class_radices[c] = it != opt.radices.end() ? it->second : choose_radices(n, prec);
     std::string msg = check_radices(n, r.class_radices[c]);
     if (!msg.empty()) return "size " + std::to_string(n) + ": " + msg;
-    tables[c] = make_pass_tables(n, r.fwd, r.class_radices[c], prec);
+  }
+  // the exact trigonometric tables of the distinct sizes, computed on all host threads
+  // (independent pure functions of (n, direction, radices)); cached ones are copied
+  std::vector<char> cached(ncls, 0);
+  if (opt.table_cache)
+    for (int c = 0; c < ncls; ++c) {
+      auto hit = opt.table_cache->find(std::make_pair(r.class_n[c], r.class_radices[c]));
+      if (hit != opt.table_cache->end()) {
+        tables[c] = hit->second;
+        cached[c] = 1;
+      }
+    }
+  {
+    std::atomic<int> next{0};
+    auto work = [&]() {
+      for (int c; (c = next.fetch_add(1)) < ncls;)
+        if (!cached[c]) tables[c] = make_pass_tables(r.class_n[c], r.fwd, r.class_radices[c], prec);
+    };
+    const int nthr = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()),
+                                             (unsigned)std::max(1, ncls / 8));
+    std::vector<std::thread> pool;
+    for (int i = 1; i < nthr; ++i) pool.emplace_back(work);
+    work();
+    for (std::thread& t : pool) t.join();
+  }
+  for (int c = 0; c < ncls; ++c) {
+    const int64_t n = r.class_n[c];
+    if (opt.table_cache && !cached[c])
+      opt.table_cache->emplace(std::make_pair(n, r.class_radices[c]), tables[c]);
     // pass grouping: the per-size strategy splits at the shared-memory limit, the persistent
     // kernel at opt.single_max; the second group's tables are stored transposed
     split_c[c] = split_point(n, r.class_radices[c],

@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -17,6 +18,9 @@ struct RaggedOptions {
   int64_t single_max = 2048;       // largest size run as one pass group
   int variant = 0;                 // block shape of the persistent kernel
   std::map<int64_t, std::vector<int>> radices;   // per-size overrides (autotuner)
+  // Pass tables by (size, radices), shared by the autotuner's candidate plans of one batch
+  // (the exact trigonometric tables dominate a plan's host time); null = no cache.
+  std::shared_ptr<std::map<std::pair<int64_t, std::vector<int>>, PassTables>> table_cache;
 };
 
 // One launch of the per-size strategy: a batched plan over one size's evenly spaced lines.

@@ -81,7 +81,10 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
   bool staged = false;   // the current item's tile has been requested into X
   __syncthreads();       // every thread has read s_next before it is overwritten
   while (it < nitems) {
-    if (threadIdx.x == 0) s_next = (int)atomicAdd(counter, 1u);   // ticket of the next item
+    // ticket of the next item: thread 0 publishes it only after the first pass, so the
+    // atomic's round trip overlaps that pass instead of delaying the CTA
+    unsigned ticket = 0;
+    if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
     const RaggedItem w = items[it];
     const RaggedClass& rc = classes[w.cls];
     int next;
@@ -90,10 +93,11 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
       const GroupDesc& g = rc.g[0];
       if (!staged) stage_item(X, g, w, in_off, in);
       cp_async_wait_all();
-      __syncthreads();   // X complete for every thread; s_next visible
-      next = s_next;
+      __syncthreads();   // X complete for every thread
       run_pass_t<double, FWD>(X, Y, w.count, g.M, g.pass[0], -1, g.nsub, g.fd_nsub);
-      __syncthreads();   // X consumed
+      if (threadIdx.x == 0) s_next = (int)ticket;
+      __syncthreads();   // X consumed; s_next visible
+      next = s_next;
       if (next < nitems) {
         const RaggedItem wn = items[next];
         const RaggedClass& rn = classes[wn.cls];
@@ -113,6 +117,7 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
       }
       copy_tile<double, false>(A, nullptr, out, g, ListedLines{in_off, out_off, w.first}, 0, w.count);
     } else {
+      if (threadIdx.x == 0) s_next = (int)ticket;
       __syncthreads();   // s_next visible
       next = s_next;
       if (next < nitems) {

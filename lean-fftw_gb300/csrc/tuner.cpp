@@ -190,12 +190,14 @@ std::string tune_ragged(RaggedPlan& r, RaggedOptions& opt) {
     int64_t tile, single;
   };
   std::vector<Cand> cands;
-  for (int v : {0, 2, 4})
-    for (int64_t t : {2048, 4096})
+  for (int v = 0; v < kRaggedVariants; ++v)
+    for (int64_t t : {1024, 2048, 4096})
       for (int64_t sm : {1024, 2048, 4096})
         cands.push_back({v, t, sm});
   float best = INFINITY;
   RaggedOptions chosen = opt;
+  RaggedOptions shared = opt;
+  shared.table_cache = std::make_shared<std::map<std::pair<int64_t, std::vector<int>>, PassTables>>();
   for (const Cand& c : cands) {
     RaggedPlan t;
     t.precision = r.precision;
@@ -205,7 +207,7 @@ std::string tune_ragged(RaggedPlan& r, RaggedOptions& opt) {
     t.sizes = r.sizes;
     t.in_off = r.in_off;
     t.out_off = r.out_off;
-    RaggedOptions o = opt;
+    RaggedOptions o = shared;
     o.variant = c.variant;
     o.tile_target = c.tile;
     o.single_max = std::min<int64_t>(c.single, max_single_group(r.precision));
@@ -227,6 +229,7 @@ std::string tune_ragged(RaggedPlan& r, RaggedOptions& opt) {
   cudaFree(out);
   if (!std::isfinite(best)) return "autotuner: no ragged candidate could be built";
   opt = chosen;
+  opt.table_cache.reset();
   return "";
 }
 

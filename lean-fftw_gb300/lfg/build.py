@@ -135,7 +135,7 @@ def compile_all(verbose: bool = False, jobs: int = 0) -> str:
             if verbose and log:
                 print(log)
     tmp = LIB + ".tmp"
-    subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs], check=True)
+    subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"], check=True)
     os.replace(tmp, LIB)
     return LIB
 

@@ -22,7 +22,8 @@ class RaggedInfo(ctypes.Structure):
                 ("grid", ctypes.c_int64), ("smem_bytes", ctypes.c_int64),
                 ("launches", ctypes.c_int64), ("in_bytes", ctypes.c_int64),
                 ("out_bytes", ctypes.c_int64), ("points", ctypes.c_int64),
-                ("flops", ctypes.c_double)]
+                ("flops", ctypes.c_double), ("tile_target", ctypes.c_int64),
+                ("single_max", ctypes.c_int64), ("block_shape", ctypes.c_int64)]
 
 
 class RaggedTuning(ctypes.Structure):
