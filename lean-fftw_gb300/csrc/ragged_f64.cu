@@ -26,44 +26,125 @@ struct FixedBases {
   __device__ int64_t pitch(bool) const { return -1; }
 };
 
-// 16-byte asynchronous copy global -> shared (completion through cp.async groups).
+// 16-byte asynchronous copy global -> shared (completion through cp.async groups).  The
+// L1-allocating form (.ca): when the source is pinned host memory read over NVLink-C2C, the
+// L2-only form (.cg) made the whole 8192-size batch 45 % slower end to end (3.24 against
+// 2.24 ms); on device memory the two are within 1 %.
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(
                    (unsigned)__cvta_generic_to_shared(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// Request the tile of a one-group item (w.count whole transforms of length g.M, each a
-// contiguous line at its listed offset) into stage buffer X, in the padded tile layout.
-__device__ __forceinline__ void stage_item(double2* X, const GroupDesc& g, const RaggedItem& w,
-                                           const int64_t* __restrict__ in_off, const double2* in) {
+// Request a tile of C sub-problems of group g, starting at sub-problem s0, from `src` into
+// stage buffer X (padded tile layout), with the element order of copy_tile's loads.
+template <class Lines>
+__device__ __forceinline__ void stage_tile(double2* X, const GroupDesc& g, const Lines& lines,
+                                           int64_t s0, int C, const double2* src) {
+  const int64_t sub_st = g.in_sub, elem_st = g.in_elem;
   const int M = g.M;
+  const int nsub = g.nsub;
+  const bool elem_fast = elem_st == 1;
+  const int64_t line0 = s0 / nsub;
+  const int sub0 = (int)(s0 - line0 * nsub);
+  const int nn = elem_fast ? C * M : g.C * M;
   const int PM = sub_pitch(M);
-  const int n = w.count * M;
-  const FastDiv fdm = g.fd_m;
-  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
-    const int c = fdiv(idx, fdm);
-    const int i = idx - c * M;
-    cp_async16(X + c * PM + spad(i), in + __ldg(in_off + w.first + c) + i);
+  for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
+    int c, i;
+    if (elem_fast) {
+      c = fdiv(idx, g.fd_m);
+      i = idx - c * M;
+    } else {
+      i = fdiv(idx, g.fd_c);
+      c = idx - i * g.C;
+      if (c >= C) continue;
+    }
+    const int t = sub0 + c;
+    const int ql = fdiv(t, g.fd_nsub);
+    const int64_t a = lines.in(line0 + ql) + (int64_t)(t - ql * nsub) * sub_st + (int64_t)i * elem_st;
+    cp_async16(X + c * PM + spad(i), src + a);
   }
   cp_async_commit();
 }
+
+// One tile of an item: its group, first sub-problem and number of sub-problems.  A one-group
+// item is one task; a two-group item is the tiles of its first group, then those of its
+// second group.
+struct Task {
+  int grp;
+  int C;
+  int64_t s0;
+};
+
+__device__ __forceinline__ int first_group_tasks(const RaggedClass& rc) {
+  return (rc.g[0].nsub + rc.g[0].C - 1) / rc.g[0].C;
+}
+__device__ __forceinline__ int task_count(const RaggedClass& rc) {
+  return rc.ngroups == 1 ? 1 : first_group_tasks(rc) + (rc.g[1].nsub + rc.g[1].C - 1) / rc.g[1].C;
+}
+__device__ __forceinline__ Task task_of(const RaggedClass& rc, const RaggedItem& w, int k) {
+  if (rc.ngroups == 1) return Task{0, w.count, 0};
+  const int n1 = first_group_tasks(rc);
+  const int grp = k < n1 ? 0 : 1;
+  const GroupDesc& g = rc.g[grp];
+  const int64_t s0 = (int64_t)(grp == 0 ? k : k - n1) * g.C;
+  return Task{grp, (int)min((int64_t)g.C, (int64_t)g.nsub - s0), s0};
+}
+
+// Where a task's tile comes from and goes to.  One group: listed lines, in -> out.  Two
+// groups: the first group reads the input line and writes the intermediate, the second reads
+// the intermediate and writes the output line; the intermediate is the output line itself, or
+// this CTA's slab `mine` of device memory when one is given (the buffers may be host memory).
+struct TaskIO {
+  const int64_t* __restrict__ in_off;
+  const int64_t* __restrict__ out_off;
+  const double2* in;
+  double2* out;
+  double2* mine;
+
+  __device__ __forceinline__ void stage(double2* X, const RaggedClass& rc, const RaggedItem& w,
+                                        const Task& t) const {
+    const GroupDesc& g = rc.g[t.grp];
+    if (rc.ngroups == 1 || (!mine && t.grp == 0)) {
+      stage_tile(X, g, ListedLines{in_off, out_off, w.first}, t.s0, t.C, in);
+    } else if (!mine) {
+      stage_tile(X, g, ListedLines{out_off, out_off, w.first}, t.s0, t.C, out);
+    } else if (t.grp == 0) {
+      stage_tile(X, g, FixedBases{__ldg(in_off + w.first), 0}, t.s0, t.C, in);
+    } else {
+      stage_tile(X, g, FixedBases{0, 0}, t.s0, t.C, mine);
+    }
+  }
+
+  __device__ __forceinline__ void store(double2* A, const RaggedClass& rc, const RaggedItem& w,
+                                        const Task& t) const {
+    const GroupDesc& g = rc.g[t.grp];
+    if (rc.ngroups == 1 || (!mine && t.grp == 0)) {
+      copy_tile<double, false>(A, nullptr, out, g, ListedLines{in_off, out_off, w.first}, t.s0, t.C);
+    } else if (!mine) {
+      copy_tile<double, false>(A, nullptr, out, g, ListedLines{out_off, out_off, w.first}, t.s0, t.C);
+    } else if (t.grp == 0) {
+      copy_tile<double, false>(A, nullptr, mine, g, FixedBases{0, 0}, t.s0, t.C);
+    } else {
+      copy_tile<double, false>(A, nullptr, out, g, FixedBases{0, __ldg(out_off + w.first)}, t.s0, t.C);
+    }
+  }
+};
 
 // Each CTA takes work items from a queue (an atomic ticket counter, zeroed before the
 // launch) until it is empty, holding one ticket ahead.  An item is a tile of up to C
 // transforms of one size (one group), or one whole transform of a two-group size.  Items
 // are sorted by decreasing cost, so the largest start first.
 //
-// Shared memory holds three tile buffers X, Y, Z of `buf` elements.  A one-group item's
-// tile arrives in X by asynchronous copies; its first pass reads X and writes Y, and as
-// soon as that pass is done the next item's tile (if it is a one-group item) is requested
-// into X, so the copies overlap the remaining passes (Y <-> Z) and the stores of the
-// current item.  A two-group item runs its two groups from Y and Z with plain tile copies:
-// the first group writes its intermediate to the output (or, when `scratch` is given, to
-// this CTA's slab of device memory, as when the buffers are host memory) and the second
-// group then works on it, the barrier between them ordering the global-memory traffic
-// within the CTA.  No CTA waits on another.
+// Shared memory holds three tile buffers X, Y, Z of `buf` elements.  Every task's tile
+// arrives in X by asynchronous copies; its first pass reads X and writes Y, and as soon as
+// that pass is done the next task's tile is requested into X (the next tile of this item,
+// or the first tile of the next item), so the copies overlap the remaining passes (Y <-> Z)
+// and the stores of the current task.  The one tile not requested ahead is the first of a
+// second group: it reads what the last tile of the first group stores, so it is requested
+// after the barrier that ends that task (a barrier orders a CTA's global-memory accesses).
+// No CTA waits on another.
 template <bool FWD, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
 ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __restrict__ items,
@@ -75,10 +156,11 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
   double2* const X = smem_f64;
   double2* const Y = smem_f64 + buf;
   double2* const Z = Y + buf;
+  const TaskIO io{in_off, out_off, in, out, scratch ? scratch + (int64_t)blockIdx.x * slab : nullptr};
   if (threadIdx.x == 0) s_next = (int)atomicAdd(counter, 1u);
   __syncthreads();
   int it = s_next;
-  bool staged = false;   // the current item's tile has been requested into X
+  bool staged = false;   // the current task's tile has been requested into X
   __syncthreads();       // every thread has read s_next before it is overwritten
   while (it < nitems) {
     // ticket of the next item: thread 0 publishes it only after the first pass, so the
@@ -87,81 +169,47 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
     if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
     const RaggedItem w = items[it];
     const RaggedClass& rc = classes[w.cls];
-    int next;
-    bool next_staged = false;
-    if (rc.ngroups == 1) {
-      const GroupDesc& g = rc.g[0];
-      if (!staged) stage_item(X, g, w, in_off, in);
+    const int nt = task_count(rc);
+    int next = nitems;
+    for (int k = 0; k < nt; ++k) {
+      const Task t = task_of(rc, w, k);
+      const GroupDesc& g = rc.g[t.grp];
+      if (!staged) io.stage(X, rc, w, t);
       cp_async_wait_all();
       __syncthreads();   // X complete for every thread
-      run_pass_t<double, FWD>(X, Y, w.count, g.M, g.pass[0], -1, g.nsub, g.fd_nsub);
-      if (threadIdx.x == 0) s_next = (int)ticket;
+      const int sub0 = g.twsub ? (int)(t.s0 % g.nsub) : -1;
+      run_pass_t<double, FWD>(X, Y, t.C, g.M, g.pass[0], sub0, g.nsub, g.fd_nsub);
+      if (k == 0 && threadIdx.x == 0) s_next = (int)ticket;
       __syncthreads();   // X consumed; s_next visible
-      next = s_next;
-      if (next < nitems) {
+      if (k == 0) next = s_next;
+      staged = false;
+      if (k + 1 < nt) {
+        const Task tn = task_of(rc, w, k + 1);
+        if (tn.grp == t.grp) {
+          io.stage(X, rc, w, tn);
+          staged = true;
+        }
+      } else if (next < nitems) {
         const RaggedItem wn = items[next];
         const RaggedClass& rn = classes[wn.cls];
-        if (rn.ngroups == 1) {
-          stage_item(X, rn.g[0], wn, in_off, in);
-          next_staged = true;
-        }
+        io.stage(X, rn, wn, task_of(rn, wn, 0));
+        staged = true;
       }
       double2* A = Y;
       double2* B = Z;
-      for (int t = 1; t < g.npass; ++t) {
-        run_pass_t<double, FWD>(A, B, w.count, g.M, g.pass[t], -1, g.nsub, g.fd_nsub);
+      for (int p = 1; p < g.npass; ++p) {
+        run_pass_t<double, FWD>(A, B, t.C, g.M, g.pass[p], sub0, g.nsub, g.fd_nsub);
         __syncthreads();
         double2* tmp = A;
         A = B;
         B = tmp;
       }
-      copy_tile<double, false>(A, nullptr, out, g, ListedLines{in_off, out_off, w.first}, 0, w.count);
-    } else {
-      if (threadIdx.x == 0) s_next = (int)ticket;
-      __syncthreads();   // s_next visible
-      next = s_next;
-      if (next < nitems) {
-        const RaggedItem wn = items[next];
-        const RaggedClass& rn = classes[wn.cls];
-        if (rn.ngroups == 1) {   // X is idle during a two-group item
-          stage_item(X, rn.g[0], wn, in_off, in);
-          next_staged = true;
-        }
-      }
-      const GroupDesc& g1 = rc.g[0];
-      const GroupDesc& g2 = rc.g[1];
-      if (scratch) {
-        // intermediate in this CTA's slab of device memory (the output may be host memory)
-        double2* mine = scratch + (int64_t)blockIdx.x * slab;
-        const FixedBases first{__ldg(in_off + w.first), 0};
-        const FixedBases second{0, __ldg(out_off + w.first)};
-        for (int64_t s0 = 0; s0 < g1.nsub; s0 += g1.C) {
-          process_tile_f64<FWD>(g1, first, s0, (int)min((int64_t)g1.C, g1.nsub - s0), in, mine, Y);
-          __syncthreads();
-        }
-        for (int64_t s0 = 0; s0 < g2.nsub; s0 += g2.C) {
-          process_tile_f64<FWD>(g2, second, s0, (int)min((int64_t)g2.C, g2.nsub - s0), mine, out, Y);
-          __syncthreads();
-        }
-      } else {
-        const ListedLines lines{in_off, out_off, w.first};
-        for (int64_t s0 = 0; s0 < g1.nsub; s0 += g1.C) {
-          process_tile_f64<FWD>(g1, lines, s0, (int)min((int64_t)g1.C, g1.nsub - s0), in, out, Y);
-          __syncthreads();
-        }
-        // the second group reads the first group's result from the output
-        const ListedLines inner{out_off, out_off, w.first};
-        for (int64_t s0 = 0; s0 < g2.nsub; s0 += g2.C) {
-          process_tile_f64<FWD>(g2, inner, s0, (int)min((int64_t)g2.C, g2.nsub - s0), out, out, Y);
-          __syncthreads();
-        }
-      }
+      io.store(A, rc, w, t);
+      __syncthreads();   // buffers free for reuse; this task's stores ordered before later loads
     }
-    __syncthreads();   // buffers free for reuse; every thread has read s_next
     it = next;
-    staged = next_staged;
   }
-  cp_async_wait_all();   // (nothing is outstanding here: a staged item is always processed)
+  cp_async_wait_all();   // (nothing is outstanding here: a requested tile is always processed)
 }
 
 constexpr int kVariant = LFG_PART / 2;
