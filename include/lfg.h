@@ -207,6 +207,19 @@ lfg_status lfg_get_ragged_info(const lfg_ragged *plan, lfg_ragged_info *info);
 /* Radix sequence used for size n (npass = 0 if n is not in the batch). */
 lfg_status lfg_get_ragged_radices(const lfg_ragged *plan, int64_t n, int *radices, int *npass);
 
+/* Tuning cache ("wisdom").  No counterpart in lean-fftw, whose measuring planner re-times
+ * every plan (LeanFFTW/Asm/Planner.lean:209-286); the calls follow FFTW's
+ * fftw_import_wisdom_from_filename / fftw_export_wisdom_to_filename / fftw_forget_wisdom.
+ * Every schedule LFG_MEASURE picks is remembered for the process, keyed by the problem, and a
+ * later LFG_MEASURE plan of the same problem reuses it without timing.  With the environment
+ * variable LFG_WISDOM naming a file, the table is read from it on first use and each new
+ * choice is appended.  Import merges a file's entries (LFG_ERR_INVALID if it cannot be read);
+ * export writes all entries; lfg_wisdom_count reports how many are held. */
+lfg_status lfg_wisdom_import(const char *path);
+lfg_status lfg_wisdom_export(const char *path);
+void lfg_wisdom_forget(void);
+size_t lfg_wisdom_count(void);
+
 /* Human-readable text of a status, and the last error message of this thread. */
 const char *lfg_strerror(lfg_status s);
 const char *lfg_last_error(void);

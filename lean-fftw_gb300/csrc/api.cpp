@@ -1313,4 +1313,20 @@ lfg_status lfg_cos_sin_table(uint64_t n, double* out) {
   return LFG_OK;
 }
 
+lfg_status lfg_wisdom_import(const char* path) {
+  if (!path) return fail(LFG_ERR_INVALID, "null path");
+  if (!lfg::wisdom_import(path)) return fail(LFG_ERR_INVALID, std::string("cannot read ") + path);
+  return LFG_OK;
+}
+
+lfg_status lfg_wisdom_export(const char* path) {
+  if (!path) return fail(LFG_ERR_INVALID, "null path");
+  if (!lfg::wisdom_export(path)) return fail(LFG_ERR_INVALID, std::string("cannot write ") + path);
+  return LFG_OK;
+}
+
+void lfg_wisdom_forget(void) { lfg::wisdom_forget(); }
+
+size_t lfg_wisdom_count(void) { return lfg::wisdom_size(); }
+
 }  // extern "C"

@@ -9,13 +9,26 @@
 // each candidate is timed with CUDA events on scratch buffers of the plan's own shape, and
 // the fastest is kept.  With LFG_PLAN_LOG set, every measured candidate is appended to that
 // file as one JSON line (the analogue of LF_PLAN_LOG, Planner.lean:162-168).
+//
+// Tuning cache ("wisdom"; lean-fftw has none and re-measures every plan): every choice the
+// autotuner makes is remembered in a process-wide table keyed by the problem (size,
+// precision, direction and scratch batch for a 1-D plan; a hash of the sizes and offsets for
+// a ragged batch), and a later LFG_MEASURE plan of the same problem takes the stored choice
+// without timing anything.  The table is read from and appended to the file named by
+// LFG_WISDOM, and lfg_wisdom_import/export/forget move it explicitly.  One entry per line:
+// `key<TAB>value`; lines starting with '#' are comments.  An entry that does not describe a
+// valid schedule for its problem is ignored and the problem is measured again.
 #include "tuner.h"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <functional>
+#include <map>
+#include <mutex>
+#include <sstream>
 
 #include "generated/opcounts.h"
 #include "kernels.h"
@@ -99,7 +112,118 @@ float time_ms(F fn, cudaStream_t s, int reps) {
   return t.empty() ? INFINITY : t[t.size() / 2];
 }
 
+
+// ---- tuning cache ---------------------------------------------------------------------------
+std::mutex g_wisdom_mu;
+std::map<std::string, std::string> g_wisdom;
+bool g_wisdom_env_read = false;
+
+bool read_wisdom_locked(const char* path) {
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char buf[8192];
+  while (std::fgets(buf, sizeof buf, f)) {
+    std::string line(buf);
+    while (!line.empty() && (line.back() == '\n' || line.back() == '\r')) line.pop_back();
+    if (line.empty() || line[0] == '#') continue;
+    const size_t tab = line.find('\t');
+    if (tab == std::string::npos || tab == 0 || tab + 1 >= line.size()) continue;
+    g_wisdom[line.substr(0, tab)] = line.substr(tab + 1);
+  }
+  std::fclose(f);
+  return true;
+}
+
+const char* wisdom_env() {
+  const char* p = std::getenv("LFG_WISDOM");
+  return p && *p ? p : nullptr;
+}
+
+void read_env_wisdom_locked() {
+  if (g_wisdom_env_read) return;
+  g_wisdom_env_read = true;
+  if (const char* p = wisdom_env()) read_wisdom_locked(p);
+}
+
+bool recall(const std::string& key, std::string* value) {
+  std::lock_guard<std::mutex> lk(g_wisdom_mu);
+  read_env_wisdom_locked();
+  auto it = g_wisdom.find(key);
+  if (it == g_wisdom.end()) return false;
+  *value = it->second;
+  return true;
+}
+
+void remember(const std::string& key, const std::string& value) {
+  std::lock_guard<std::mutex> lk(g_wisdom_mu);
+  read_env_wisdom_locked();
+  g_wisdom[key] = value;
+  if (const char* p = wisdom_env())
+    if (FILE* f = std::fopen(p, "a")) {
+      std::fprintf(f, "%s\t%s\n", key.c_str(), value.c_str());
+      std::fclose(f);
+    }
+}
+
+// value fields "name=v1,v2,...;name=..." -> integers of one field (empty if absent or malformed)
+std::vector<int64_t> field(const std::string& value, const char* name) {
+  std::vector<int64_t> out;
+  const std::string tag = std::string(name) + "=";
+  size_t pos = 0;
+  while (pos < value.size()) {
+    size_t end = value.find(';', pos);
+    if (end == std::string::npos) end = value.size();
+    if (value.compare(pos, tag.size(), tag) == 0) {
+      std::stringstream ss(value.substr(pos + tag.size(), end - pos - tag.size()));
+      std::string tok;
+      while (std::getline(ss, tok, ',')) {
+        char* e = nullptr;
+        const long long v = std::strtoll(tok.c_str(), &e, 10);
+        if (tok.empty() || *e) return {};
+        out.push_back(v);
+      }
+      return out;
+    }
+    pos = end + 1;
+  }
+  return out;
+}
+
+uint64_t fnv1a(uint64_t h, const void* p, size_t bytes) {
+  const unsigned char* c = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < bytes; ++i) h = (h ^ c[i]) * 1099511628211ull;
+  return h;
+}
+
 }  // namespace
+
+bool wisdom_import(const char* path) {
+  std::lock_guard<std::mutex> lk(g_wisdom_mu);
+  read_env_wisdom_locked();
+  return read_wisdom_locked(path);
+}
+
+bool wisdom_export(const char* path) {
+  std::lock_guard<std::mutex> lk(g_wisdom_mu);
+  read_env_wisdom_locked();
+  FILE* f = std::fopen(path, "w");
+  if (!f) return false;
+  std::fprintf(f, "# lean-fftw GB300 tuning cache: key<TAB>value\n");
+  for (const auto& kv : g_wisdom) std::fprintf(f, "%s\t%s\n", kv.first.c_str(), kv.second.c_str());
+  return std::fclose(f) == 0;
+}
+
+void wisdom_forget() {
+  std::lock_guard<std::mutex> lk(g_wisdom_mu);
+  g_wisdom.clear();
+  g_wisdom_env_read = true;   // a forgotten table is not re-read from LFG_WISDOM
+}
+
+size_t wisdom_size() {
+  std::lock_guard<std::mutex> lk(g_wisdom_mu);
+  read_env_wisdom_locked();
+  return g_wisdom.size();
+}
 
 std::string tune_c2c(Plan& p, int64_t default_tile) {
   const int prec = p.precision;
@@ -108,6 +232,22 @@ std::string tune_c2c(Plan& p, int64_t default_tile) {
   const int64_t per_line = p.n;
   int64_t lines = std::max<int64_t>(1, std::min<int64_t>(p.howmany, ((int64_t)256 << 20) / (per_line * es)));
   lines = std::max<int64_t>(lines, std::min<int64_t>(p.howmany, ((int64_t)32 << 20) / (per_line * es)));
+  const std::string key = "c2c n=" + std::to_string(p.n) + " precision=" + std::to_string(prec) +
+                          " fwd=" + std::to_string(p.fwd ? 1 : 0) + " lines=" + std::to_string(lines);
+  {
+    std::string v;
+    if (recall(key, &v)) {
+      const std::vector<int64_t> rs = field(v, "radices"), sm = field(v, "single"), tl = field(v, "tile");
+      std::vector<int> r(rs.begin(), rs.end());
+      if (!rs.empty() && sm.size() == 1 && tl.size() == 1 && check_radices(p.n, r).empty() &&
+          sm[0] >= 2 && tl[0] >= 16 && tl[0] <= 65536) {
+        p.radices = r;
+        p.single_max = sm[0];
+        p.tile = tl[0];
+        return "";
+      }
+    }
+  }
   void *din = nullptr, *dout = nullptr;
   const size_t bytes = (size_t)lines * per_line * es;
   if (cudaMalloc(&din, bytes) != cudaSuccess) return "autotuner: scratch allocation failed";
@@ -171,11 +311,41 @@ std::string tune_c2c(Plan& p, int64_t default_tile) {
   p.radices = chosen.radices;
   p.single_max = chosen.single_max;
   p.tile = best_tile;
+  std::string rs;
+  for (size_t i = 0; i < p.radices.size(); ++i) rs += (i ? "," : "") + std::to_string(p.radices[i]);
+  remember(key, "radices=" + rs + ";single=" + std::to_string(p.single_max) + ";tile=" +
+                    std::to_string(p.tile));
   return "";
 }
 
 std::string tune_ragged(RaggedPlan& r, RaggedOptions& opt) {
   const size_t es = r.precision == 0 ? 16 : 8;
+  uint64_t h = 1469598103934665603ull;
+  h = fnv1a(h, r.sizes.data(), r.sizes.size() * sizeof(int64_t));
+  h = fnv1a(h, r.in_off.data(), r.in_off.size() * sizeof(int64_t));
+  h = fnv1a(h, r.out_off.data(), r.out_off.size() * sizeof(int64_t));
+  for (const auto& kv : opt.radices) {
+    h = fnv1a(h, &kv.first, sizeof kv.first);
+    h = fnv1a(h, kv.second.data(), kv.second.size() * sizeof(int));
+  }
+  char hex[17];
+  std::snprintf(hex, sizeof hex, "%016llx", (unsigned long long)h);
+  const std::string key = "ragged precision=" + std::to_string(r.precision) + " fwd=" +
+                          std::to_string(r.fwd ? 1 : 0) + " count=" + std::to_string(r.sizes.size()) +
+                          " hash=" + hex;
+  {
+    std::string v;
+    if (recall(key, &v)) {
+      const std::vector<int64_t> sh = field(v, "shape"), tl = field(v, "tile"), sm = field(v, "single");
+      if (sh.size() == 1 && tl.size() == 1 && sm.size() == 1 && sh[0] >= 0 &&
+          sh[0] < kRaggedVariants && tl[0] >= 16 && tl[0] <= 65536 && sm[0] >= 2) {
+        opt.variant = (int)sh[0];
+        opt.tile_target = tl[0];
+        opt.single_max = std::min<int64_t>(sm[0], max_single_group(r.precision));
+        return "";
+      }
+    }
+  }
   void *in = nullptr, *out = nullptr;
   if (cudaMalloc(&in, (size_t)r.in_span * es) != cudaSuccess) return "autotuner: scratch allocation failed";
   if (cudaMalloc(&out, (size_t)r.out_span * es) != cudaSuccess) {
@@ -230,6 +400,8 @@ std::string tune_ragged(RaggedPlan& r, RaggedOptions& opt) {
   if (!std::isfinite(best)) return "autotuner: no ragged candidate could be built";
   opt = chosen;
   opt.table_cache.reset();
+  remember(key, "shape=" + std::to_string(opt.variant) + ";tile=" + std::to_string(opt.tile_target) +
+                    ";single=" + std::to_string(opt.single_max));
   return "";
 }
 

@@ -20,4 +20,11 @@ std::string tune_c2c(Plan& p, int64_t default_tile);
 // on success `opt` holds the fastest.
 std::string tune_ragged(RaggedPlan& r, RaggedOptions& opt);
 
+// Tuning cache (tuner.cpp): both tuners consult it before timing anything and record what
+// they choose.  Import merges a file's entries, export writes every entry, forget empties it.
+bool wisdom_import(const char* path);
+bool wisdom_export(const char* path);
+void wisdom_forget();
+size_t wisdom_size();
+
 }  // namespace lfg

@@ -178,3 +178,23 @@ def cos_sin_table(n: int) -> np.ndarray:
     out = np.empty(2 * n, dtype=np.float64)
     check(lib().lfg_cos_sin_table(n, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
     return out.reshape(n, 2)
+
+
+def wisdom_import(path: str) -> None:
+    """Merge the tuning-cache entries of a file (lfg_wisdom_import)."""
+    check(lib().lfg_wisdom_import(str(path).encode()))
+
+
+def wisdom_export(path: str) -> None:
+    """Write every tuning-cache entry to a file (lfg_wisdom_export)."""
+    check(lib().lfg_wisdom_export(str(path).encode()))
+
+
+def wisdom_forget() -> None:
+    """Empty the process's tuning cache (lfg_wisdom_forget)."""
+    lib().lfg_wisdom_forget()
+
+
+def wisdom_count() -> int:
+    """Entries held in the process's tuning cache (lfg_wisdom_count)."""
+    return int(lib().lfg_wisdom_count())
