@@ -342,7 +342,9 @@ lfg_status finish_real(lfg::Plan& p, const lfg::RealLayout& L, lfg_plan** out) {
   p.in_span = r2c ? rspan : cspan;
   p.out_span = r2c ? cspan : rspan;
   if (!p.empty) {
-    if ((e = lfg::prepare_group_kernels_f64()) != cudaSuccess) return cuda_fail(e, "kernel set-up");
+    // the column pass of a rank-2 plan runs the group kernels of the plan's precision
+    e = p.precision == 0 ? lfg::prepare_group_kernels_f64() : lfg::prepare_group_kernels_f32();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel set-up");
     if ((e = lfg::prepare_real_kernels()) != cudaSuccess) return cuda_fail(e, "kernel set-up");
     std::string msg = lfg::build_real(p, L, tile_target());
     if (!msg.empty()) {

@@ -87,6 +87,7 @@ struct Plan {
   // (asynchronous copies of the next tile), one grid per group
   bool tile_stream = false;
   unsigned ts_grid[2] = {0, 0};
+  unsigned col_ts_grid = 0;     // binary32 column pass of a rank-2 real plan: persistent grid
   int* d_status = nullptr; // set to 1 on the device when a bounded wait gave up
   // real transforms (kind R2C / C2R): rows of the last dimension, and for rank 2 the complex
   // transform along the first dimension (columns of the half spectrum)
@@ -163,6 +164,10 @@ size_t smem_bytes(int64_t C, int64_t M, int precision);
 int64_t max_single_group(int precision);
 // Index after the last pass of the first group (rs.size() for a single group), balancing the
 // two groups' lengths, both at most max_m; -1 if impossible.
+// Store each pass table as (re, im) pairs: row pair (2r, 2r+1) of ns values becomes ns
+// pairs, so a butterfly reads each twiddle with one vector load.  Compensated binary32 tables
+// interleave their hi and lo halves separately.  Applied after transpose_second_group.
+void interleave_tables(PassTables& pt, const std::vector<int>& rs, const std::vector<int>& comp);
 int split_point(int64_t N, const std::vector<int>& rs, int64_t max_m);
 // Fill the passes and tile size of a group covering passes t0..t1-1; tw_base is the device
 // copy of PassTables::values.

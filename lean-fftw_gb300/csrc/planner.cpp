@@ -182,6 +182,23 @@ void transpose_second_group(PassTables& pt, const std::vector<int>& rs, int spli
   }
 }
 
+void interleave_tables(PassTables& pt, const std::vector<int>& rs, const std::vector<int>& comp) {
+  std::vector<double> pairs;
+  for (size_t t = 1; t < rs.size(); ++t) {
+    const int64_t ns = pt.ns[t];
+    const int parts = !comp.empty() && comp[t] ? 2 : 1;   // hi table, then lo table
+    for (int part = 0; part < parts; ++part) {
+      double* v = pt.values.data() + pt.offset[t] + (size_t)part * 2 * (rs[t] - 1) * ns;
+      pairs.assign(v, v + 2 * (size_t)(rs[t] - 1) * ns);
+      for (int r = 0; r < rs[t] - 1; ++r)
+        for (int64_t k = 0; k < ns; ++k) {
+          v[2 * ((size_t)r * ns + k)] = pairs[(size_t)(2 * r) * ns + k];
+          v[2 * ((size_t)r * ns + k) + 1] = pairs[(size_t)(2 * r + 1) * ns + k];
+        }
+    }
+  }
+}
+
 int split_point(int64_t N, const std::vector<int>& rs, int64_t max_m) {
   if (N <= max_m) return (int)rs.size();
   int best = -1;
@@ -329,6 +346,7 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   const std::vector<int> comp = compensated_passes(N, rs, split, p.no_comp ? 0 : prec);
   if (prec == 1) pt.values = split_compensated(pt, rs, comp);
   transpose_second_group(pt, rs, split, comp);
+  interleave_tables(pt, rs, comp);
   p.d_twiddles = upload_tables(pt.values, prec, &msg);
   if (!p.d_twiddles) return msg;
 
@@ -455,6 +473,7 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
     msg = check_radices(M, p.radices);
     if (!msg.empty()) return msg;
     pt = make_pass_tables(M, r2c, p.radices, prec);
+    interleave_tables(pt, p.radices, {});
   }
   p.d_twiddles = upload_tables(pt.values, prec, &msg);
   if (!p.d_twiddles) return msg;
@@ -494,12 +513,15 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
     if (!msg.empty()) return msg;
     if (L.n0 > max_m) return "first dimension too large for one pass group";
     PassTables ct = make_pass_tables(L.n0, r2c, crs, prec);
+    interleave_tables(ct, crs, {});
     p.d_col_twiddles = upload_tables(ct.values, prec, &msg);
     if (!p.d_col_twiddles) return msg;
     const int64_t h = M + 1;
     GroupDesc& g = p.col;
     fill_group(g, crs, ct, 0, (int)crs.size(), 1, tile_target, prec, p.d_col_twiddles);
     int64_t cm = std::max<int64_t>(1, tile_target / L.n0);
+    // columns are copied as runs of C neighbouring elements: keep binary32 runs at 64 bytes
+    if (prec == 1) cm = std::max<int64_t>(cm, 8);
     while (cm > 1 && smem_bytes(cm, L.n0, prec) > kSmemBudget) --cm;
     // columns of one image are the sub-problems; tiles may straddle images (no sub-problem
     // index enters the twiddles of a single group)
@@ -525,6 +547,18 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
       d.c_rdist = h;
     }
     p.flops += plan_ops(L.n0, crs) * (double)(L.howmany * h);
+    // binary32 columns: the persistent strided-tile kernel (the next tile's elements copied
+    // asynchronously under the current tile's passes) when its three tile buffers fit
+    if (prec == 1 && smem_bytes(g.C, g.M, prec) / 2 * 3 <= kSmemBudget) {
+      int dev = 0, sms = 1;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      GroupDesc gs = g;
+      set_divisors(gs);
+      const int64_t tiles = (g.total_sub + g.C - 1) / g.C;
+      const int64_t want = (int64_t)sms * tile_stream_blocks_per_sm_f32(gs);
+      p.col_ts_grid = (unsigned)std::max<int64_t>(1, std::min(want, tiles));
+    }
   }
   return "";
 }
@@ -625,6 +659,8 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
   const size_t es = p.precision == 0 ? 16 : 8;
   auto launch_col = [&](bool fwd, const void* a, void* b) -> cudaError_t {
     if (p.precision == 0) return launch_group_f64(p.col, fwd, a, b, stream);
+    if (p.col_ts_grid && ((uintptr_t)a % 8) == 0 && ((uintptr_t)b % 8) == 0)
+      return launch_tile_stream_f32(p.col, fwd, a, b, p.col_ts_grid, stream);
     return launch_group_f32(p.col, fwd, a, b, stream);
   };
   if (p.kind == Kind::R2C) {

@@ -120,6 +120,7 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
                                              : std::min(opt.single_max, ragged_max_single_group()));
     if (split_c[c] < 0) return "size " + std::to_string(n) + " needs more than two pass groups";
     transpose_second_group(tables[c], r.class_radices[c], split_c[c], {});
+    interleave_tables(tables[c], r.class_radices[c], {});
     base[c] = total;
     total += tables[c].values.size();
     r.flops += plan_ops(n, r.class_radices[c]) * (double)r.class_count[c];

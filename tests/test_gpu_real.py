@@ -162,3 +162,20 @@ def test_fp32_rank2_64x512x512():
     torch.cuda.synchronize()
     r = y.cpu().numpy() / (n0 * n1)
     assert np.max(np.abs(r - x)) < 64 * U32, np.max(np.abs(r - x))
+
+
+def test_fp32_rank2_in_fresh_process():
+    """A binary32 rank-2 real plan must set up its own kernels: run it in a process that has
+    made no other plan (kernel attributes are per process)."""
+    import subprocess
+    import sys
+    from conftest import ROOT
+    code = ("import sys; sys.path.insert(0, 'lean-fftw_gb300'); import numpy as np, torch, lfg\n"
+            "x = torch.rand(8, 512, 512, device='cuda') - 0.5\n"
+            "out = torch.empty((8, 512, 257), dtype=torch.complex64, device='cuda')\n"
+            "lfg.plan_r2c_2d(512, 512, 8, precision='f32').execute(x, out)\n"
+            "ref = np.fft.rfft2(x.cpu().numpy().astype(np.float64))\n"
+            "e = np.linalg.norm(out.cpu().numpy() - ref) / np.linalg.norm(ref)\n"
+            "assert e < 8 * 2.0 ** -24, e\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
