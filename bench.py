@@ -339,10 +339,17 @@ def main():
     ap.add_argument("--untuned", action="store_true",
                     help="ragged: plan with the default schedule instead of autotuning it "
                          "(profiling runs, where the tuner's candidate launches would be captured)")
+    ap.add_argument("--precision", choices=["f64", "f32"], default=None,
+                    help="c2c workloads: compute in this precision (the sweep's binary32 leg); "
+                         "binary32 batches double so each size still moves 1 GiB")
     ap.add_argument("--batch", type=int, default=0,
                     help="override the batch of a c2c workload (smaller cases for profiling)")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload])
+    if args.precision and wl["kind"] == "c2c" and wl.get("precision", "f64") != args.precision:
+        wl["precision"] = args.precision
+        if args.precision == "f32" and args.workload.startswith("c2c_") and wl["batch"] > 1:
+            wl["batch"] *= 2
     if args.batch > 0 and "batch" in wl:
         wl["batch"] = args.batch
     if args.impl == "reference":

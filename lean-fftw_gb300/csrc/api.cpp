@@ -175,6 +175,7 @@ lfg_status build_c2c_device(lfg::Plan& p) {
   // binary64 is bound by the FP64 pipe: two groups of small tiles (more CTAs per SM) beat one
   // group with a CTA-sized tile above 2048 points; binary32 is bound by HBM: as few groups as fit
   if (p.single_max == 0 && p.precision == 0) p.single_max = single_max_default();
+  if (p.single_max == 0 && p.precision == 1) p.single_max = lfg::kF32SingleGroupMax;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");

@@ -135,6 +135,10 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target);
 // Radix sequence with the fewest codelet operations for size n (first pass untwiddled),
 // or an empty vector when n is not 13-smooth.
 std::vector<int> choose_radices(int64_t n, int precision);
+// Largest binary32 size run as one pass group by default.  Binary32 is bound by HBM, and a
+// one-group tile above this size leaves one CTA per SM; larger sizes run two groups of about
+// sqrt(n) points each (choose_radices orders the radices for that split).
+constexpr int64_t kF32SingleGroupMax = 8192;
 
 // Codelet operation count of a plan's radix sequence, per transform.
 double plan_ops(int64_t n, const std::vector<int>& radices);

@@ -76,8 +76,28 @@ size_t smem_bytes(int64_t C, int64_t M, int precision) {
 }
 
 std::vector<int> choose_radices(int64_t n, int precision) {
-  (void)precision;
   if (n < 2) return {};
+  if (precision == 1 && n > kF32SingleGroupMax) {
+    // binary32 two-group sizes: the fewest operations for each factor of the most balanced
+    // split n = P * Q (split_point then cuts there), so both groups get tiles of ~sqrt(n)
+    int64_t bestP = 0;
+    double bestd = INFINITY;
+    for (int64_t P = 2; P * P <= n; ++P) {
+      if (n % P) continue;
+      const double d = std::fabs(std::log((double)P) - std::log((double)(n / P)));
+      if (d < bestd) {
+        bestd = d;
+        bestP = P;
+      }
+    }
+    if (bestP > 0) {
+      std::vector<int> a = choose_radices(n / bestP, 0), b = choose_radices(bestP, 0);
+      if (!a.empty() && !b.empty()) {
+        a.insert(a.end(), b.begin(), b.end());
+        return a;
+      }
+    }
+  }
   std::map<int64_t, Best> memo;
   double best = INFINITY;
   std::vector<int> seq;
@@ -565,8 +585,7 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
 
 // The intermediate buffer of in-place two-group execution (one block of lines), allocated on
 // first use and kept by the plan.
-static cudaError_t ensure_scratch(const Plan& p) {
-  const size_t need = (size_t)p.n * (size_t)p.howmany * (p.precision == 0 ? 16 : 8);
+static cudaError_t ensure_scratch_bytes(const Plan& p, size_t need) {
   if (p.scratch_bytes >= need) return cudaSuccess;
   if (p.d_scratch) cudaFree(p.d_scratch);
   p.d_scratch = nullptr;
@@ -574,6 +593,10 @@ static cudaError_t ensure_scratch(const Plan& p) {
   cudaError_t e = cudaMalloc(&p.d_scratch, need);
   if (e == cudaSuccess) p.scratch_bytes = need;
   return e;
+}
+
+static cudaError_t ensure_scratch(const Plan& p) {
+  return ensure_scratch_bytes(p, (size_t)p.n * (size_t)p.howmany * (p.precision == 0 ? 16 : 8));
 }
 
 cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream,
@@ -664,6 +687,15 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     return launch_group_f32(p.col, fwd, a, b, stream);
   };
   if (p.kind == Kind::R2C) {
+    if (force_scratch && p.has_col) {
+      // host-mapped buffers: the rows go to a device copy of the output span and the column
+      // pass reads them there, so the half spectrum crosses the host link once
+      cudaError_t e = ensure_scratch_bytes(p, (size_t)p.out_span * (p.precision == 0 ? 8 : 4));
+      if (e != cudaSuccess) return e;
+      if ((e = launch_real(p.real, p.precision, true, in, p.d_scratch, stream)) != cudaSuccess) return e;
+      const int64_t off = p.real.c_off * (int64_t)es;
+      return launch_col(true, static_cast<char*>(p.d_scratch) + off, static_cast<char*>(out) + off);
+    }
     cudaError_t e = launch_real(p.real, p.precision, true, in, out, stream);
     if (e != cudaSuccess || !p.has_col) return e;
     char* ob = static_cast<char*>(out) + p.real.c_off * (int64_t)es;

@@ -260,8 +260,12 @@ std::string tune_c2c(Plan& p, int64_t default_tile) {
   cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
 
   std::vector<std::vector<int>> seqs = candidate_radices(p.n, 1.15, 6);
+  if (prec == 1) {   // the balanced binary32 order (choose_radices) is always a candidate
+    const std::vector<int> bal = choose_radices(p.n, prec);
+    if (std::find(seqs.begin(), seqs.end(), bal) == seqs.end()) seqs.push_back(bal);
+  }
   std::vector<int64_t> splits = prec == 0 ? std::vector<int64_t>{1024, 2048, 4096, 1 << 30}
-                                          : std::vector<int64_t>{1 << 30};
+                                          : std::vector<int64_t>{kF32SingleGroupMax, 1 << 30};
   std::vector<int64_t> tiles = {1024, 2048, 4096};
   float best = INFINITY;
   Plan chosen;
