@@ -21,6 +21,11 @@ namespace dev {
 template <class T>
 struct Prec;
 
+// 1.0 and -0.0 for the binary64 codelets' fused forms of a + b and a * b (generated
+// codelets: a*1 + b and a*b + (-0) round exactly as the add and the multiply).  They are read
+// through a volatile load in each pass so the compiler cannot fold the fused forms back.
+static __device__ double lfg_fma_units[2] = {1.0, -0.0};
+
 template <>
 struct Prec<double> {
   using C = double2;
@@ -31,6 +36,11 @@ struct Prec<double> {
   static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
   static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+  static __device__ __forceinline__ void units(double& one, double& nz) {
+    const volatile double* u = lfg_fma_units;
+    one = u[0];
+    nz = u[1];
+  }
 };
 
 template <>
@@ -43,6 +53,10 @@ struct Prec<float> {
   static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
   static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
   static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+  static __device__ __forceinline__ void units(float& one, float& nz) {   // unused by binary32
+    one = 1.0f;
+    nz = -0.0f;
+  }
 };
 
 
@@ -94,6 +108,8 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
   const int nsg = pd.ns_g;             // < 2^24: products with r stay in int
   const FastDiv fd_mr = pd.fd_mr, fd_ns = pd.fd_ns;
   const int PM = sub_pitch(M);
+  T one, nz;
+  P::units(one, nz);
   for (int q = threadIdx.x; q < nb; q += blockDim.x) {
     const int c = fdiv(q, fd_mr);
     const int j = q - c * MR;
@@ -140,7 +156,7 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
         x[2 * r + 1] = P::fma(a, wih, P::fma(bi, wrh, ci));
       }
     }
-    P::template Bfly<FWD, R, TW>::run(x, y);
+    P::template Bfly<FWD, R, TW>::run(x, y, one, nz);
     const int d0 = b * ns * R + k;
     Cx* dc = out.row(c);
 #pragma unroll
