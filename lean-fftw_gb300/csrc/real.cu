@@ -33,20 +33,23 @@ __device__ __forceinline__ int64_t cplx_base(const RealDesc& d, int64_t line) {
   return d.c_off + b * d.c_bdist + r * d.c_rdist;   // complex elements
 }
 
+// Additions and multiplications of the split epilogue / prologue; binary64 uses the fused
+// forms of the codelets (a*1 + b, a*b + (-0): the same values, at the DFMA issue rate).
 template <class T>
-struct RealOps {
-  static __device__ __forceinline__ T add(T a, T b);
-  static __device__ __forceinline__ T sub(T a, T b);
-};
+struct RealOps;
 template <>
 struct RealOps<double> {
-  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  double one, nz;
+  __device__ __forceinline__ RealOps() { Prec<double>::units(one, nz); }
+  __device__ __forceinline__ double add(double a, double b) const { return __fma_rn(a, one, b); }
+  __device__ __forceinline__ double sub(double a, double b) const { return __fma_rn(-b, one, a); }
+  __device__ __forceinline__ double mul(double a, double b) const { return __fma_rn(a, b, nz); }
 };
 template <>
 struct RealOps<float> {
-  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+  __device__ __forceinline__ float add(float a, float b) const { return __fadd_rn(a, b); }
+  __device__ __forceinline__ float sub(float a, float b) const { return __fsub_rn(a, b); }
+  __device__ __forceinline__ float mul(float a, float b) const { return __fmul_rn(a, b); }
 };
 
 template <class T>
@@ -54,6 +57,7 @@ __global__ void __launch_bounds__(kGroupThreads)
 r2c_kernel(const RealDesc d, const T* in, typename Prec<T>::C* out) {
   using P = Prec<T>;
   using O = RealOps<T>;
+  const O ops;
   using Cx = typename P::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx* smem = reinterpret_cast<Cx*>(smem_raw);
@@ -81,16 +85,16 @@ r2c_kernel(const RealDesc d, const T* in, typename Prec<T>::C* out) {
     Cx* o = out + cplx_base(d, l0 + c);
     if (k == 0) {
       const Cx z = Fc[0];
-      o[0] = P::mk(O::add(z.x, z.y), T(0));
-      o[M] = P::mk(O::sub(z.x, z.y), T(0));
+      o[0] = P::mk(ops.add(z.x, z.y), T(0));
+      o[M] = P::mk(ops.sub(z.x, z.y), T(0));
       continue;
     }
     const Cx a = Fc[spad(k)], bc = Fc[spad(M - k)];
-    const T sr = O::add(a.x, bc.x), si = O::sub(a.y, bc.y);
-    const T dr = O::sub(a.x, bc.x), di = O::add(a.y, bc.y);
+    const T sr = ops.add(a.x, bc.x), si = ops.sub(a.y, bc.y);
+    const T dr = ops.sub(a.x, bc.x), di = ops.add(a.y, bc.y);
     const Cx w = __ldg(tw + k);
-    const T Pp = P::fma(w.x, di, -P::mul(w.y, dr));   // (c di - s dr) / 2
-    const T Q = P::fma(w.y, di, P::mul(w.x, dr));     // (s di + c dr) / 2
+    const T Pp = P::fma(w.x, di, -ops.mul(w.y, dr));   // (c di - s dr) / 2
+    const T Q = P::fma(w.y, di, ops.mul(w.x, dr));     // (s di + c dr) / 2
     o[k] = P::mk(P::fma(hf, sr, Pp), P::fma(hf, si, -Q));
     if (k != M - k) o[M - k] = P::mk(P::fma(hf, sr, -Pp), P::fma(-hf, si, -Q));
   }
@@ -101,6 +105,7 @@ __global__ void __launch_bounds__(kGroupThreads)
 c2r_kernel(const RealDesc d, const typename Prec<T>::C* in, T* out) {
   using P = Prec<T>;
   using O = RealOps<T>;
+  const O ops;
   using Cx = typename P::C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx* smem = reinterpret_cast<Cx*>(smem_raw);
@@ -119,21 +124,21 @@ c2r_kernel(const RealDesc d, const typename Prec<T>::C* in, T* out) {
     Cx* Ac = A + c * PM;
     if (k == 0) {
       const T h0 = h[0].x, hm = h[M].x;   // imaginary parts ignored
-      Ac[0] = P::mk(O::add(h0, hm), O::sub(h0, hm));
+      Ac[0] = P::mk(ops.add(h0, hm), ops.sub(h0, hm));
       continue;
     }
     Cx a = h[k], bc = h[M - k];
     if (d.adjoint) {   // halve the bins 1..M-1 (exact)
-      a = P::mk(P::mul(a.x, T(0.5)), P::mul(a.y, T(0.5)));
-      bc = P::mk(P::mul(bc.x, T(0.5)), P::mul(bc.y, T(0.5)));
+      a = P::mk(ops.mul(a.x, T(0.5)), ops.mul(a.y, T(0.5)));
+      bc = P::mk(ops.mul(bc.x, T(0.5)), ops.mul(bc.y, T(0.5)));
     }
-    const T sr = O::add(a.x, bc.x), si = O::sub(a.y, bc.y);
-    const T dr = O::sub(a.x, bc.x), di = O::add(a.y, bc.y);
+    const T sr = ops.add(a.x, bc.x), si = ops.sub(a.y, bc.y);
+    const T dr = ops.sub(a.x, bc.x), di = ops.add(a.y, bc.y);
     const Cx w = __ldg(tw + k);
-    const T U = P::fma(w.x, di, P::mul(w.y, dr));    // c di + s dr
-    const T V = P::fma(w.x, dr, -P::mul(w.y, di));   // c dr - s di
-    Ac[spad(k)] = P::mk(O::sub(sr, U), O::add(si, V));
-    if (k != M - k) Ac[spad(M - k)] = P::mk(O::add(sr, U), O::sub(V, si));
+    const T U = P::fma(w.x, di, ops.mul(w.y, dr));    // c di + s dr
+    const T V = P::fma(w.x, dr, -ops.mul(w.y, di));   // c dr - s di
+    Ac[spad(k)] = P::mk(ops.sub(sr, U), ops.add(si, V));
+    if (k != M - k) Ac[spad(M - k)] = P::mk(ops.add(sr, U), ops.sub(V, si));
   }
   __syncthreads();
   const Cx* F = run_passes<T, false>(g, A, B, C, -1);

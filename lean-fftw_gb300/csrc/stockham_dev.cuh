@@ -22,8 +22,9 @@ template <class T>
 struct Prec;
 
 // 1.0 and -0.0 for the binary64 codelets' fused forms of a + b and a * b (generated
-// codelets: a*1 + b and a*b + (-0) round exactly as the add and the multiply).  They are read
-// through a volatile load in each pass so the compiler cannot fold the fused forms back.
+// codelets: a*1 + b and a*b + (-0) round exactly as the add and the multiply).  Each pass
+// reads them with an opaque non-coherent load (inline PTX, served by L1), so the compiler
+// cannot fold the fused forms back into DADD/DMUL.
 static __device__ double lfg_fma_units[2] = {1.0, -0.0};
 
 template <>
@@ -37,9 +38,9 @@ struct Prec<double> {
   static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
   static __device__ __forceinline__ double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
   static __device__ __forceinline__ void units(double& one, double& nz) {
-    const volatile double* u = lfg_fma_units;
-    one = u[0];
-    nz = u[1];
+    const size_t a = __cvta_generic_to_global(lfg_fma_units);
+    asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(one) : "l"(a));
+    asm volatile("ld.global.nc.f64 %0, [%1+8];" : "=d"(nz) : "l"(a));
   }
 };
 
