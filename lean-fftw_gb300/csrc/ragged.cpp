@@ -41,6 +41,46 @@ void free_ragged(RaggedPlan& r) {
   if (cur != r.device) cudaSetDevice(cur);
 }
 
+namespace {
+
+// Operations of a tile of C sub-problems of length M through passes t0..t1 of rs, and the
+// lane-slots they occupy: a pass of nb = C * M / R butterflies issues ceil(nb / 32) warps,
+// so a partial last warp leaves lanes of the FP64 pipe idle.
+void tile_lane_cost(int64_t C, int64_t M, const std::vector<int>& rs, int t0, int t1,
+                    double* ops, double* slots) {
+  for (int t = t0; t < t1; ++t) {
+    const int R = rs[t];
+    const int64_t nb = C * (M / R);
+    const double o = t == 0 ? kOpsUntw[R] : kOpsTw[R];
+    *ops += (double)nb * o;
+    *slots += (double)(32 * ((nb + 31) / 32)) * o;
+  }
+}
+
+// Tile width for `total` sub-problems in tiles of at most cmax: the C in [cmax/2, cmax] whose
+// tiles (and last, partial tile) waste the fewest lanes; ties to the wider tile.
+int64_t lane_efficient_width(int64_t M, const std::vector<int>& rs, int t0, int t1, int64_t total,
+                             int64_t cmax) {
+  int64_t best = cmax;
+  double best_eff = -1;
+  for (int64_t C = cmax; C >= std::max<int64_t>(1, cmax / 2); --C) {
+    double ops = 0, slots = 0;
+    const int64_t full = total / C, rem = total % C;
+    tile_lane_cost(C, M, rs, t0, t1, &ops, &slots);
+    ops *= (double)full;
+    slots *= (double)full;
+    if (rem) tile_lane_cost(rem, M, rs, t0, t1, &ops, &slots);
+    const double eff = slots > 0 ? ops / slots : 0;
+    if (eff > best_eff + 1e-12) {
+      best_eff = eff;
+      best = C;
+    }
+  }
+  return best;
+}
+
+}  // namespace
+
 std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
   const int prec = r.precision;
   const int64_t count = (int64_t)r.sizes.size();
@@ -152,7 +192,9 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
       fill_group(g, rs, tables[c], 0, (int)rs.size(), 1, opt.tile_target, prec, tw);
       int64_t cmax = std::max<int64_t>(1, opt.tile_target / n);
       while (cmax > 1 && !ragged_tile_fits(cmax, n)) --cmax;
-      g.C = (int)std::min<int64_t>(cmax, r.class_count[c]);
+      cmax = std::min<int64_t>(cmax, r.class_count[c]);
+      g.C = (int)(r.per_size_mode ? cmax
+                                  : lane_efficient_width(n, rs, 0, (int)rs.size(), r.class_count[c], cmax));
       g.in_sub = g.out_sub = 0;
       g.in_elem = g.out_elem = 1;
       g.total_sub = g.C;
@@ -181,6 +223,15 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
       g2.out_elem = P;
       g1.total_sub = Q;
       g2.total_sub = P;
+      if (!r.per_size_mode) {   // tile widths that leave the fewest warp lanes idle
+        for (GroupDesc* g : {&g1, &g2}) {
+          int64_t cmax = std::max<int64_t>(1, opt.tile_target / g->M);
+          while (cmax > 1 && !ragged_tile_fits(cmax, g->M)) --cmax;
+          cmax = std::min<int64_t>(cmax, g->nsub);
+          const int t0 = g == &g1 ? 0 : split, t1 = g == &g1 ? split : (int)rs.size();
+          g->C = (int)lane_efficient_width(g->M, rs, t0, t1, g->nsub, cmax);
+        }
+      }
       for (int64_t i = 0; i < r.class_count[c]; ++i) {
         items.push_back(RaggedItem{c, 1, r.class_first[c] + i});
         item_cost.push_back(ops_one);
