@@ -92,6 +92,22 @@ __device__ __forceinline__ Task task_of(const RaggedClass& rc, const RaggedItem&
   return Task{grp, (int)min((int64_t)g.C, (int64_t)g.nsub - s0), s0};
 }
 
+// Destination of a last pass that writes global memory directly: sub-problem c of the tile
+// (starting at sub-problem s0 of its line list) is a contiguous run at this address.
+template <class Lines>
+struct GlobalOut {
+  double2* dst;
+  const GroupDesc& g;
+  Lines lines;
+  int64_t s0;
+  __device__ __forceinline__ double2* row(int c) const {
+    const int t = (int)s0 + c;   // s0 < nsub < 2^31 (one line per task, or lines of one tile)
+    const int ql = fdiv(t, g.fd_nsub);
+    return dst + lines.out(ql) + (int64_t)(t - ql * g.nsub) * g.out_sub;
+  }
+  __device__ __forceinline__ void put(double2* row, int i, double2 v) const { row[i] = v; }
+};
+
 // Where a task's tile comes from and goes to.  One group: listed lines, in -> out.  Two
 // groups: the first group reads the input line and writes the intermediate, the second reads
 // the intermediate and writes the output line; the intermediate is the output line itself, or
@@ -114,6 +130,29 @@ struct TaskIO {
       stage_tile(X, g, FixedBases{__ldg(in_off + w.first), 0}, t.s0, t.C, in);
     } else {
       stage_tile(X, g, FixedBases{0, 0}, t.s0, t.C, mine);
+    }
+  }
+
+  // Tasks whose outputs are contiguous runs per sub-problem (one-group items, first groups)
+  // let their last pass store straight to global memory: consecutive threads write
+  // consecutive elements of a run, and the tile's round trip through shared memory, with
+  // its barrier, disappears.
+  __device__ __forceinline__ bool direct(const RaggedClass& rc, const Task& t) const {
+    const GroupDesc& g = rc.g[t.grp];
+    return (rc.ngroups == 1 || t.grp == 0) && g.out_elem == 1 && g.scale == 1.0;
+  }
+
+  template <bool FWD>
+  __device__ __forceinline__ void last_pass(const double2* A, const RaggedClass& rc,
+                                            const RaggedItem& w, const Task& t, const PassDesc& pd,
+                                            int sub0) const {
+    const GroupDesc& g = rc.g[t.grp];
+    if (mine && rc.ngroups == 2) {
+      run_pass_to<double, FWD>(A, GlobalOut<FixedBases>{mine, g, FixedBases{0, 0}, t.s0}, t.C, g.M,
+                               pd, sub0, g.nsub, g.fd_nsub);
+    } else {
+      run_pass_to<double, FWD>(A, GlobalOut<ListedLines>{out, g, ListedLines{in_off, out_off, w.first}, t.s0},
+                               t.C, g.M, pd, sub0, g.nsub, g.fd_nsub);
     }
   }
 
@@ -178,7 +217,10 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
       cp_async_wait_all();
       __syncthreads();   // X complete for every thread
       const int sub0 = g.twsub ? (int)(t.s0 % g.nsub) : -1;
-      run_pass_t<double, FWD>(X, Y, t.C, g.M, g.pass[0], sub0, g.nsub, g.fd_nsub);
+      const bool direct = io.direct(rc, t);
+      const int np = g.npass;
+      if (np == 1 && direct) io.template last_pass<FWD>(X, rc, w, t, g.pass[0], sub0);
+      else run_pass_t<double, FWD>(X, Y, t.C, g.M, g.pass[0], sub0, g.nsub, g.fd_nsub);
       if (k == 0 && threadIdx.x == 0) s_next = (int)ticket;
       __syncthreads();   // X consumed; s_next visible
       if (k == 0) next = s_next;
@@ -197,14 +239,18 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
       }
       double2* A = Y;
       double2* B = Z;
-      for (int p = 1; p < g.npass; ++p) {
+      for (int p = 1; p < np; ++p) {
+        if (p == np - 1 && direct) {
+          io.template last_pass<FWD>(A, rc, w, t, g.pass[p], sub0);
+          break;
+        }
         run_pass_t<double, FWD>(A, B, t.C, g.M, g.pass[p], sub0, g.nsub, g.fd_nsub);
         __syncthreads();
         double2* tmp = A;
         A = B;
         B = tmp;
       }
-      io.store(A, rc, w, t);
+      if (!direct) io.store(A, rc, w, t);
       __syncthreads();   // buffers free for reuse; this task's stores ordered before later loads
     }
     it = next;
