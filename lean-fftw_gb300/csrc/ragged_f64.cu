@@ -92,22 +92,6 @@ __device__ __forceinline__ Task task_of(const RaggedClass& rc, const RaggedItem&
   return Task{grp, (int)min((int64_t)g.C, (int64_t)g.nsub - s0), s0};
 }
 
-// Destination of a last pass that writes global memory directly: sub-problem c of the tile
-// (starting at sub-problem s0 of its line list) is a contiguous run at this address.
-template <class Lines>
-struct GlobalOut {
-  double2* dst;
-  const GroupDesc& g;
-  Lines lines;
-  int64_t s0;
-  __device__ __forceinline__ double2* row(int c) const {
-    const int t = (int)s0 + c;   // s0 < nsub < 2^31 (one line per task, or lines of one tile)
-    const int ql = fdiv(t, g.fd_nsub);
-    return dst + lines.out(ql) + (int64_t)(t - ql * g.nsub) * g.out_sub;
-  }
-  __device__ __forceinline__ void put(double2* row, int i, double2 v) const { row[i] = v; }
-};
-
 // Where a task's tile comes from and goes to.  One group: listed lines, in -> out.  Two
 // groups: the first group reads the input line and writes the intermediate, the second reads
 // the intermediate and writes the output line; the intermediate is the output line itself, or
@@ -148,10 +132,11 @@ struct TaskIO {
                                             int sub0) const {
     const GroupDesc& g = rc.g[t.grp];
     if (mine && rc.ngroups == 2) {
-      run_pass_to<double, FWD>(A, GlobalOut<FixedBases>{mine, g, FixedBases{0, 0}, t.s0}, t.C, g.M,
-                               pd, sub0, g.nsub, g.fd_nsub);
+      run_pass_to<double, FWD>(A, GlobalRows<double, FixedBases>{mine, g, FixedBases{0, 0}, 0, (int)t.s0},
+                               t.C, g.M, pd, sub0, g.nsub, g.fd_nsub);
     } else {
-      run_pass_to<double, FWD>(A, GlobalOut<ListedLines>{out, g, ListedLines{in_off, out_off, w.first}, t.s0},
+      run_pass_to<double, FWD>(A, GlobalRows<double, ListedLines>{out, g, ListedLines{in_off, out_off, w.first},
+                                                                  0, (int)t.s0},
                                t.C, g.M, pd, sub0, g.nsub, g.fd_nsub);
     }
   }
