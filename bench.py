@@ -331,7 +331,7 @@ def make_flush(dev):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=600)   # ~1 s timed: several clock samples
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="ragged", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="lfg", choices=["lfg", "reference"])
@@ -474,7 +474,7 @@ def main():
         ps_step = lambda: per_size.execute(x, y2)
         for _ in range(3):
             ps_step()
-        ps_ms, _ = timed(ps_step, max(5, args.steps // 4), stream, local, barrier)
+        ps_ms, _ = timed(ps_step, min(20, max(5, args.steps // 4)), stream, local, barrier)
         ps_ms = max_over_ranks(ps_ms, dev)
         torch.cuda.synchronize()
         extra["per_size"] = {"value": round(flops_step * ws / (ps_ms * 1e-3) / 1e9, 3),
