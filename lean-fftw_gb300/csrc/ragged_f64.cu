@@ -1,8 +1,9 @@
 // Persistent FP64 kernel over a ragged batch (one launch for all sizes).
 //
 // The kernel exists in kRaggedVariants block shapes and two directions; each of those ten
-// instantiations carries the codelets of every radix three times over (one per tile
-// source), so the build compiles this file once per instantiation, with -DLFG_PART=p
+// instantiations carries the codelets of every radix three times over (one per pass
+// destination: shared memory, or the output rows of a line list or of a scratch slab), so
+// the build compiles this file once per instantiation, with -DLFG_PART=p
 // (p = 2 * variant + (forward ? 1 : 0)), in parallel.  stockham_f64.cu gathers the parts.
 #include <cuda_runtime.h>
 
