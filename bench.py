@@ -438,7 +438,7 @@ def main():
             xg = torch.from_numpy(a).to(dev, non_blocking=True).requires_grad_(True)
             loss = torch.sum(torch.abs(W * torch_ops.fft(xg)) ** 2)
             loss.backward()
-            b[...] = xg.grad.cpu().numpy()
+            torch.from_numpy(b).copy_(xg.grad)        # device -> pinned host, then synchronise
 
         extra["config_extra"] = {"loss": "sum |W * FFT(x)|^2", "radices": fplan.radices}
     else:
