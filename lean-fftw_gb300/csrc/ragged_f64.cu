@@ -124,7 +124,7 @@ struct TaskIO {
   // its barrier, disappears.
   __device__ __forceinline__ bool direct(const RaggedClass& rc, const Task& t) const {
     const GroupDesc& g = rc.g[t.grp];
-    return (rc.ngroups == 1 || t.grp == 0) && g.out_elem == 1 && g.scale == 1.0;
+    return (rc.ngroups == 1 || t.grp == 0) && g.out_elem == 1 && g.unit_scale;
   }
 
   template <bool FWD>

@@ -99,6 +99,8 @@ struct GroupDesc {
   int kmul;              // product of the radices before the group (P for a second group)
   int twsub;
   double scale;          // outputs multiplied by this on store unless it is exactly 1
+  int unit_scale;        // scale == 1 (set_divisors: kernels test it without an FP64 compare)
+  float scale_f32;       // scale rounded to binary32 (set_divisors)
   FastDiv fd_m, fd_c, fd_nsub;   // divisors M, C, nsub (set_divisors)
   PassDesc pass[kMaxPass];
 };
@@ -106,6 +108,8 @@ struct GroupDesc {
 // Fill the FastDiv fields from M, C, nsub and the passes; every launch path calls this on
 // the descriptor it passes to a kernel, so planners may change C freely before.
 inline void set_divisors(GroupDesc& g) {
+  g.unit_scale = g.scale == 1.0 ? 1 : 0;
+  g.scale_f32 = (float)g.scale;
   g.fd_m = make_fastdiv(g.M > 0 ? g.M : 1);
   g.fd_c = make_fastdiv(g.C > 0 ? g.C : 1);
   g.fd_nsub = make_fastdiv(g.nsub > 0 ? g.nsub : 1);

@@ -238,7 +238,7 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
   const int nsub = g.nsub;
   const int n = C * M;
   const bool elem_fast = (elem_st == 1);
-  if (elem_fast && nsub == 1 && lines.pitch(LOAD) == M && g.scale == 1.0) {
+  if (elem_fast && nsub == 1 && lines.pitch(LOAD) == M && g.unit_scale) {
     // back-to-back lines: the tile is one contiguous range of global memory
     const int64_t base = (LOAD ? lines.in(s0) : lines.out(s0));
     const int PM = sub_pitch(M);
@@ -256,8 +256,8 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
   // strided sub-problems: neighbouring threads take neighbouring sub-problems, over the full
   // tile width g.C (a partial last tile skips the missing columns)
   const int nn = elem_fast ? n : g.C * M;
-  const bool unit = g.scale == 1.0;
-  const T sc = (T)g.scale;
+  const bool unit = g.unit_scale != 0;
+  const T sc = sizeof(T) == 4 ? (T)g.scale_f32 : (T)g.scale;
   const int PM = sub_pitch(M);
   for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
     int c, i;

@@ -142,7 +142,7 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
     // store the tile (contiguous): two complex values per 16-byte store
     float4* o4 = reinterpret_cast<float4*>(out + l0 * M);
     const int n4 = C * M / 2;
-    const float sc = (float)g.scale;
+    const float sc = g.scale_f32;
     const bool flat = (M & 15) == 0;   // then c * PM + spad(ii) = spad(c * M + ii)
     for (int i = threadIdx.x; i < n4; i += blockDim.x) {
       const int e = 2 * i;
@@ -156,7 +156,7 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
         t1 = c * PM + spad(ii + 1);
       }
       const float2 a = src[t0], b = src[t1];
-      if (g.scale == 1.0) o4[i] = make_float4(a.x, a.y, b.x, b.y);
+      if (g.unit_scale) o4[i] = make_float4(a.x, a.y, b.x, b.y);
       else o4[i] = make_float4(__fmul_rn(a.x, sc), __fmul_rn(a.y, sc), __fmul_rn(b.x, sc), __fmul_rn(b.y, sc));
     }
     __syncthreads();
