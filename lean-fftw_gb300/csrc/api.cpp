@@ -413,6 +413,7 @@ lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision prec
   if (radices) {
     if (npass < 1 || npass > lfg::kMaxPass) return fail(LFG_ERR_INVALID, "bad pass count");
     p.radices.assign(radices, radices + npass);
+    p.radices_given = true;
   } else {
     p.radices = lfg::choose_radices(p.n, precision);
   }

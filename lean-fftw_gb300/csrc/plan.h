@@ -80,6 +80,7 @@ struct Plan {
   bool no_comp = false;    // binary32: no compensated twiddle passes
   int64_t tile = 0;        // complex elements per CTA tile (0: the default)
   bool measure = false;    // LFG_MEASURE: autotune before building
+  bool radices_given = false;   // the caller fixed the radix sequence (never reordered)
   // binary32 single-group plans over back-to-back lines run the persistent bulk-copy kernel
   bool stream = false;
   unsigned stream_grid = 0;
@@ -135,6 +136,9 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target);
 // Radix sequence with the fewest codelet operations for size n (first pass untwiddled),
 // or an empty vector when n is not 13-smooth.
 std::vector<int> choose_radices(int64_t n, int precision);
+// The fewest-operation radices of each factor of the most balanced split n = P * Q (larger
+// factor first), so split_point cuts at P; empty if n is prime or not 13-smooth.
+std::vector<int> balanced_radices(int64_t n);
 // Largest binary32 size run as one pass group by default.  Binary32 is bound by HBM, and a
 // one-group tile above this size leaves one CTA per SM; larger sizes run two groups of about
 // sqrt(n) points each (choose_radices orders the radices for that split).

@@ -75,28 +75,30 @@ size_t smem_bytes(int64_t C, int64_t M, int precision) {
   return 2 * (size_t)tile_elems(C, (int)M) * (precision == 0 ? 16 : 8);
 }
 
+std::vector<int> balanced_radices(int64_t n) {
+  int64_t bestP = 0;
+  double bestd = INFINITY;
+  for (int64_t P = 2; P * P <= n; ++P) {
+    if (n % P) continue;
+    const double d = std::fabs(std::log((double)P) - std::log((double)(n / P)));
+    if (d < bestd) {
+      bestd = d;
+      bestP = P;
+    }
+  }
+  if (bestP == 0) return {};
+  std::vector<int> a = choose_radices(n / bestP, 0), b = choose_radices(bestP, 0);
+  if (a.empty() || b.empty()) return {};
+  a.insert(a.end(), b.begin(), b.end());
+  return a;
+}
+
 std::vector<int> choose_radices(int64_t n, int precision) {
   if (n < 2) return {};
   if (precision == 1 && n > kF32SingleGroupMax) {
-    // binary32 two-group sizes: the fewest operations for each factor of the most balanced
-    // split n = P * Q (split_point then cuts there), so both groups get tiles of ~sqrt(n)
-    int64_t bestP = 0;
-    double bestd = INFINITY;
-    for (int64_t P = 2; P * P <= n; ++P) {
-      if (n % P) continue;
-      const double d = std::fabs(std::log((double)P) - std::log((double)(n / P)));
-      if (d < bestd) {
-        bestd = d;
-        bestP = P;
-      }
-    }
-    if (bestP > 0) {
-      std::vector<int> a = choose_radices(n / bestP, 0), b = choose_radices(bestP, 0);
-      if (!a.empty() && !b.empty()) {
-        a.insert(a.end(), b.begin(), b.end());
-        return a;
-      }
-    }
+    // binary32 two-group sizes: both groups get tiles of ~sqrt(n) points
+    std::vector<int> b = balanced_radices(n);
+    if (!b.empty()) return b;
   }
   std::map<int64_t, Best> memo;
   double best = INFINITY;
@@ -360,7 +362,18 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   // sequence after the prefix whose product P best balances P against N/P
   const int64_t single = p.single_max > 0 ? std::min(p.single_max, max_single_group(prec))
                                           : max_single_group(prec);
-  const int split = split_point(N, rs, single);
+  int split = split_point(N, rs, single);
+  // no split within the preferred group size: allow groups up to the shared-memory limit, and
+  // (for a planner-chosen order) reorder the radices around the most balanced factor pair
+  if (split < 0) split = split_point(N, rs, max_single_group(prec));
+  if (split < 0 && !p.radices_given) {
+    std::vector<int> bal = balanced_radices(N);
+    const int s2 = bal.empty() ? -1 : split_point(N, bal, max_single_group(prec));
+    if (s2 >= 0) {
+      rs = bal;
+      split = s2;
+    }
+  }
   if (split < 0) return "size too large for two pass groups with this radix order";
   PassTables pt = make_pass_tables(N, p.fwd, rs, prec);
   const std::vector<int> comp = compensated_passes(N, rs, split, p.no_comp ? 0 : prec);
