@@ -138,9 +138,15 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
     }
   {
     std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
     auto work = [&]() {
-      for (int c; (c = next.fetch_add(1)) < ncls;)
-        if (!cached[c]) tables[c] = make_pass_tables(r.class_n[c], r.fwd, r.class_radices[c], prec);
+      try {
+        for (int c; (c = next.fetch_add(1)) < ncls;)
+          if (!cached[c]) tables[c] = make_pass_tables(r.class_n[c], r.fwd, r.class_radices[c], prec);
+      } catch (...) {   // (host allocation) reported below, never thrown across the thread
+        failed = true;
+        next = ncls;
+      }
     };
     const int nthr = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()),
                                              (unsigned)std::max(1, ncls / 8));
@@ -148,6 +154,7 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
     for (int i = 1; i < nthr; ++i) pool.emplace_back(work);
     work();
     for (std::thread& t : pool) t.join();
+    if (failed) return "host allocation for the twiddle tables failed";
   }
   for (int c = 0; c < ncls; ++c) {
     const int64_t n = r.class_n[c];
