@@ -151,7 +151,13 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
     const int nthr = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()),
                                              (unsigned)std::max(1, ncls / 8));
     std::vector<std::thread> pool;
-    for (int i = 1; i < nthr; ++i) pool.emplace_back(work);
+    for (int i = 1; i < nthr; ++i) {
+      try {
+        pool.emplace_back(work);
+      } catch (...) {   // no more threads: the calling thread does the rest
+        break;
+      }
+    }
     work();
     for (std::thread& t : pool) t.join();
     if (failed) return "host allocation for the twiddle tables failed";
