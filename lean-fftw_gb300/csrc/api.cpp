@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <new>
 #include <string>
 
@@ -822,38 +823,52 @@ lfg_status plan_rdft2_packed(bool r2c, const std::vector<SDim>& T, const std::ve
   return wrap_plan(p, out);
 }
 
+// Runs an entry point's body, turning C++ exceptions into statuses.
+template <class F>
+lfg_status guarded(F&& body) {
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    return fail(LFG_ERR_NOMEM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(LFG_ERR_INVALID, std::string("internal error: ") + e.what());
+  } catch (...) {
+    return fail(LFG_ERR_INVALID, "internal error");
+  }
+}
+
 }  // namespace
 
 void lfg::set_last_error(const std::string& msg) { g_last_error = msg; }
 
 extern "C" {
 
-lfg_status lfg_plan_1d(size_t n, int sign, size_t howmany, lfg_precision precision,
+static lfg_status lfg_plan_1d_impl(size_t n, int sign, size_t howmany, lfg_precision precision,
                        unsigned flags, lfg_plan** out) {
   return plan_1d_common(n, sign, howmany, precision, nullptr, 0, out, flags);
 }
 
-lfg_status lfg_plan_r2c(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
+static lfg_status lfg_plan_r2c_impl(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
                         lfg_plan** out) {
   return plan_real_common(true, 1, n, howmany, precision, flags, out);
 }
 
-lfg_status lfg_plan_c2r(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
+static lfg_status lfg_plan_c2r_impl(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
                         lfg_plan** out) {
   return plan_real_common(false, 1, n, howmany, precision, flags, out);
 }
 
-lfg_status lfg_plan_r2c_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
+static lfg_status lfg_plan_r2c_2d_impl(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
                            unsigned flags, lfg_plan** out) {
   return plan_real_common(true, n0, n1, howmany, precision, flags, out);
 }
 
-lfg_status lfg_plan_c2r_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
+static lfg_status lfg_plan_c2r_2d_impl(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
                            unsigned flags, lfg_plan** out) {
   return plan_real_common(false, n0, n1, howmany, precision, flags, out);
 }
 
-lfg_status lfg_plan_r2r(size_t n, int kind, size_t howmany, lfg_precision precision,
+static lfg_status lfg_plan_r2r_impl(size_t n, int kind, size_t howmany, lfg_precision precision,
                         unsigned flags, lfg_plan** out) {
   if (!out) return fail(LFG_ERR_INVALID, "null output handle");
   *out = nullptr;
@@ -864,7 +879,7 @@ lfg_status lfg_plan_r2r(size_t n, int kind, size_t howmany, lfg_precision precis
   return plan_separable(true, T, V, {kind}, 0, 0, -1, precision, flags, out);
 }
 
-lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision precision,
+static lfg_status lfg_plan_1d_radices_impl(size_t n, int sign, size_t howmany, lfg_precision precision,
                                const int* radices, int npass, lfg_plan** out) {
   if (!radices) return fail(LFG_ERR_INVALID, "null radices");
   return plan_1d_common(n, sign, howmany, precision, radices, npass, out);
@@ -872,7 +887,7 @@ lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision
 
 // Decode lean-fftw's problem encoding (LeanFFTW/FFI.lean:32-47) and plan the parts this
 // library executes.  Strides and offsets arrive in doubles.
-lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precision,
+static lfg_status lfg_plan_spec_impl(const double* spec, size_t nspec, lfg_precision precision,
                          unsigned flags, lfg_plan** out) {
   if (!out) return fail(LFG_ERR_INVALID, "null output handle");
   *out = nullptr;
@@ -1014,7 +1029,7 @@ lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precisi
   return finish_c2c(p, out);
 }
 
-lfg_status lfg_execute(const lfg_plan* plan, const void* in, void* out, void* stream) {
+static lfg_status lfg_execute_impl(const lfg_plan* plan, const void* in, void* out, void* stream) {
   if (!plan) return fail(LFG_ERR_INVALID, "null plan");
   if (plan->p.empty) return LFG_OK;
   if (!in || !out) return fail(LFG_ERR_INVALID, "null buffer");
@@ -1025,7 +1040,7 @@ lfg_status lfg_execute(const lfg_plan* plan, const void* in, void* out, void* st
   return LFG_OK;
 }
 
-lfg_status lfg_execute_host(const lfg_plan* plan, const void* in, void* out) {
+static lfg_status lfg_execute_host_impl(const lfg_plan* plan, const void* in, void* out) {
   if (!plan) return fail(LFG_ERR_INVALID, "null plan");
   const lfg::Plan& p = plan->p;
   if (p.empty) return LFG_OK;
@@ -1068,7 +1083,7 @@ void lfg_destroy(lfg_plan* plan) {
   delete plan;
 }
 
-lfg_status lfg_set_scale(lfg_plan* plan, double scale) {
+static lfg_status lfg_set_scale_impl(lfg_plan* plan, double scale) {
   if (!plan) return fail(LFG_ERR_INVALID, "null plan");
   if (!std::isfinite(scale)) return fail(LFG_ERR_INVALID, "scale must be finite");
   lfg::Plan& p = plan->p;
@@ -1088,7 +1103,7 @@ lfg_status lfg_set_scale(lfg_plan* plan, double scale) {
   return LFG_OK;
 }
 
-lfg_status lfg_device_status(const lfg_plan* plan) {
+static lfg_status lfg_device_status_impl(const lfg_plan* plan) {
   if (!plan) return fail(LFG_ERR_INVALID, "null plan");
   const lfg::Plan& p = plan->p;
   if (!p.d_status) return LFG_OK;
@@ -1102,7 +1117,7 @@ lfg_status lfg_device_status(const lfg_plan* plan) {
   return LFG_OK;
 }
 
-lfg_status lfg_get_plan_info(const lfg_plan* plan, lfg_plan_info* info) {
+static lfg_status lfg_get_plan_info_impl(const lfg_plan* plan, lfg_plan_info* info) {
   if (!plan || !info) return fail(LFG_ERR_INVALID, "null argument");
   const lfg::Plan& p = plan->p;
   std::memset(info, 0, sizeof *info);
@@ -1119,7 +1134,7 @@ lfg_status lfg_get_plan_info(const lfg_plan* plan, lfg_plan_info* info) {
   return LFG_OK;
 }
 
-lfg_status lfg_plan_ragged(const int64_t* sizes, size_t count, const int64_t* in_offsets,
+static lfg_status lfg_plan_ragged_impl(const int64_t* sizes, size_t count, const int64_t* in_offsets,
                            const int64_t* out_offsets, int sign, lfg_precision precision,
                            unsigned flags, const lfg_ragged_tuning* tuning, lfg_ragged** out) {
   if (!out) return fail(LFG_ERR_INVALID, "null output handle");
@@ -1206,7 +1221,7 @@ lfg_status lfg_plan_ragged(const int64_t* sizes, size_t count, const int64_t* in
   return LFG_OK;
 }
 
-lfg_status lfg_execute_ragged(const lfg_ragged* plan, const void* in, void* out, void* stream) {
+static lfg_status lfg_execute_ragged_impl(const lfg_ragged* plan, const void* in, void* out, void* stream) {
   if (!plan) return fail(LFG_ERR_INVALID, "null plan");
   if (plan->r.empty) return LFG_OK;
   if (!in || !out) return fail(LFG_ERR_INVALID, "null buffer");
@@ -1218,7 +1233,7 @@ lfg_status lfg_execute_ragged(const lfg_ragged* plan, const void* in, void* out,
   return LFG_OK;
 }
 
-lfg_status lfg_execute_ragged_host(const lfg_ragged* plan, const void* in, void* out) {
+static lfg_status lfg_execute_ragged_host_impl(const lfg_ragged* plan, const void* in, void* out) {
   if (!plan) return fail(LFG_ERR_INVALID, "null plan");
   const lfg::RaggedPlan& r = plan->r;
   if (r.empty) return LFG_OK;
@@ -1258,7 +1273,7 @@ void lfg_destroy_ragged(lfg_ragged* plan) {
   delete plan;
 }
 
-lfg_status lfg_get_ragged_info(const lfg_ragged* plan, lfg_ragged_info* info) {
+static lfg_status lfg_get_ragged_info_impl(const lfg_ragged* plan, lfg_ragged_info* info) {
   if (!plan || !info) return fail(LFG_ERR_INVALID, "null argument");
   const lfg::RaggedPlan& r = plan->r;
   std::memset(info, 0, sizeof *info);
@@ -1284,7 +1299,7 @@ lfg_status lfg_get_ragged_info(const lfg_ragged* plan, lfg_ragged_info* info) {
   return LFG_OK;
 }
 
-lfg_status lfg_get_ragged_radices(const lfg_ragged* plan, int64_t n, int* radices, int* npass) {
+static lfg_status lfg_get_ragged_radices_impl(const lfg_ragged* plan, int64_t n, int* radices, int* npass) {
   if (!plan || !radices || !npass) return fail(LFG_ERR_INVALID, "null argument");
   const lfg::RaggedPlan& r = plan->r;
   *npass = 0;
@@ -1310,20 +1325,20 @@ const char* lfg_strerror(lfg_status s) {
 
 const char* lfg_last_error(void) { return g_last_error.c_str(); }
 
-lfg_status lfg_cos_sin_table(uint64_t n, double* out) {
+static lfg_status lfg_cos_sin_table_impl(uint64_t n, double* out) {
   if (!out || n == 0) return fail(LFG_ERR_INVALID, "bad arguments");
   std::vector<double> t = lfg::cos_sin_2pi_table(n);
   std::memcpy(out, t.data(), t.size() * sizeof(double));
   return LFG_OK;
 }
 
-lfg_status lfg_wisdom_import(const char* path) {
+static lfg_status lfg_wisdom_import_impl(const char* path) {
   if (!path) return fail(LFG_ERR_INVALID, "null path");
   if (!lfg::wisdom_import(path)) return fail(LFG_ERR_INVALID, std::string("cannot read ") + path);
   return LFG_OK;
 }
 
-lfg_status lfg_wisdom_export(const char* path) {
+static lfg_status lfg_wisdom_export_impl(const char* path) {
   if (!path) return fail(LFG_ERR_INVALID, "null path");
   if (!lfg::wisdom_export(path)) return fail(LFG_ERR_INVALID, std::string("cannot write ") + path);
   return LFG_OK;
@@ -1333,4 +1348,104 @@ void lfg_wisdom_forget(void) { lfg::wisdom_forget(); }
 
 size_t lfg_wisdom_count(void) { return lfg::wisdom_size(); }
 
+
+// The exported entry points: every C++ exception (host allocation failures above all) is
+// turned into a status here, so none crosses the C ABI.
+
+lfg_status lfg_plan_1d(size_t n, int sign, size_t howmany, lfg_precision precision,
+                       unsigned flags, lfg_plan** out) {
+  return guarded([&] { return lfg_plan_1d_impl(n, sign, howmany, precision, flags, out); });
+}
+
+lfg_status lfg_plan_r2c(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
+                        lfg_plan** out) {
+  return guarded([&] { return lfg_plan_r2c_impl(n, howmany, precision, flags, out); });
+}
+
+lfg_status lfg_plan_c2r(size_t n, size_t howmany, lfg_precision precision, unsigned flags,
+                        lfg_plan** out) {
+  return guarded([&] { return lfg_plan_c2r_impl(n, howmany, precision, flags, out); });
+}
+
+lfg_status lfg_plan_r2c_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
+                           unsigned flags, lfg_plan** out) {
+  return guarded([&] { return lfg_plan_r2c_2d_impl(n0, n1, howmany, precision, flags, out); });
+}
+
+lfg_status lfg_plan_c2r_2d(size_t n0, size_t n1, size_t howmany, lfg_precision precision,
+                           unsigned flags, lfg_plan** out) {
+  return guarded([&] { return lfg_plan_c2r_2d_impl(n0, n1, howmany, precision, flags, out); });
+}
+
+lfg_status lfg_plan_r2r(size_t n, int kind, size_t howmany, lfg_precision precision,
+                        unsigned flags, lfg_plan** out) {
+  return guarded([&] { return lfg_plan_r2r_impl(n, kind, howmany, precision, flags, out); });
+}
+
+lfg_status lfg_plan_1d_radices(size_t n, int sign, size_t howmany, lfg_precision precision,
+                               const int* radices, int npass, lfg_plan** out) {
+  return guarded([&] { return lfg_plan_1d_radices_impl(n, sign, howmany, precision, radices, npass, out); });
+}
+
+lfg_status lfg_plan_spec(const double* spec, size_t nspec, lfg_precision precision,
+                         unsigned flags, lfg_plan** out) {
+  return guarded([&] { return lfg_plan_spec_impl(spec, nspec, precision, flags, out); });
+}
+
+lfg_status lfg_execute(const lfg_plan* plan, const void* in, void* out, void* stream) {
+  return guarded([&] { return lfg_execute_impl(plan, in, out, stream); });
+}
+
+lfg_status lfg_execute_host(const lfg_plan* plan, const void* in, void* out) {
+  return guarded([&] { return lfg_execute_host_impl(plan, in, out); });
+}
+
+lfg_status lfg_set_scale(lfg_plan* plan, double scale) {
+  return guarded([&] { return lfg_set_scale_impl(plan, scale); });
+}
+
+lfg_status lfg_device_status(const lfg_plan* plan) {
+  return guarded([&] { return lfg_device_status_impl(plan); });
+}
+
+lfg_status lfg_get_plan_info(const lfg_plan* plan, lfg_plan_info* info) {
+  return guarded([&] { return lfg_get_plan_info_impl(plan, info); });
+}
+
+lfg_status lfg_plan_ragged(const int64_t* sizes, size_t count, const int64_t* in_offsets,
+                           const int64_t* out_offsets, int sign, lfg_precision precision,
+                           unsigned flags, const lfg_ragged_tuning* tuning, lfg_ragged** out) {
+  return guarded([&] {
+    return lfg_plan_ragged_impl(sizes, count, in_offsets, out_offsets, sign, precision, flags,
+                                tuning, out);
+  });
+}
+
+lfg_status lfg_execute_ragged(const lfg_ragged* plan, const void* in, void* out, void* stream) {
+  return guarded([&] { return lfg_execute_ragged_impl(plan, in, out, stream); });
+}
+
+lfg_status lfg_execute_ragged_host(const lfg_ragged* plan, const void* in, void* out) {
+  return guarded([&] { return lfg_execute_ragged_host_impl(plan, in, out); });
+}
+
+lfg_status lfg_get_ragged_info(const lfg_ragged* plan, lfg_ragged_info* info) {
+  return guarded([&] { return lfg_get_ragged_info_impl(plan, info); });
+}
+
+lfg_status lfg_get_ragged_radices(const lfg_ragged* plan, int64_t n, int* radices, int* npass) {
+  return guarded([&] { return lfg_get_ragged_radices_impl(plan, n, radices, npass); });
+}
+
+lfg_status lfg_cos_sin_table(uint64_t n, double* out) {
+  return guarded([&] { return lfg_cos_sin_table_impl(n, out); });
+}
+
+lfg_status lfg_wisdom_import(const char* path) {
+  return guarded([&] { return lfg_wisdom_import_impl(path); });
+}
+
+lfg_status lfg_wisdom_export(const char* path) {
+  return guarded([&] { return lfg_wisdom_export_impl(path); });
+}
 }  // extern "C"
