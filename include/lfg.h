@@ -8,7 +8,10 @@
  * Conventions (lean-fftw docs/CONTRACT.md): unnormalised transforms; forward = sign -1;
  * complex data interleaved (re, im) unless a split layout is given by the spec's offsets.
  * Every entry point returns an lfg_status; unsupported problems return LFG_ERR_UNSUPPORTED
- * and never compute a different transform (lean-fftw docs/CONTRACT.md:44-45).
+ * and never compute a different transform (lean-fftw docs/CONTRACT.md:44-45).  No C++
+ * exception crosses this interface (host allocation failures return LFG_ERR_NOMEM).  Data
+ * pointers must be aligned to a complex element: 16 bytes for binary64, 8 for binary32
+ * (LFG_ERR_INVALID otherwise, before anything runs).
  */
 #ifndef LFG_H
 #define LFG_H
