@@ -87,7 +87,8 @@ def fp64_peak():
 
 
 PROFILE_OF = {"ragged": "ragged_kernel_f64_ragged8192.md",
-              "c2c_1024": "group_kernel_f64_c2c1024.md"}
+              "c2c_1024": "group_kernel_f64_c2c1024.md",
+              "c2c_1024_f32": "stream_kernel_f32_c2c1024.md"}
 
 
 def ncu_traffic(workload):
