@@ -223,6 +223,15 @@ lfg_status lfg_wisdom_export(const char *path);
 void lfg_wisdom_forget(void);
 size_t lfg_wisdom_count(void);
 
+/* The radix sequence and pass grouping a default 1-D plan of size n would use, computed on
+ * the host only (no device is touched): the analogue of printing the chosen plan with
+ * LF_PLAN_SHOW (LeanFFTW/Asm/Planner.lean:299-300) without building it.  radices: room for 24
+ * ints; *npass = the sequence length; *first_group = the passes of the first pass group
+ * (*npass for a single group).  Sizes with a prime factor above 13 (generic or Bluestein
+ * paths) and sizes outside 2..2^24 return LFG_ERR_UNSUPPORTED. */
+lfg_status lfg_plan_layout(size_t n, lfg_precision precision, int *radices, int *npass,
+                           int *first_group);
+
 /* Human-readable text of a status, and the last error message of this thread. */
 const char *lfg_strerror(lfg_status s);
 const char *lfg_last_error(void);

@@ -1332,6 +1332,24 @@ static lfg_status lfg_cos_sin_table_impl(uint64_t n, double* out) {
   return LFG_OK;
 }
 
+static lfg_status lfg_plan_layout_impl(size_t n, lfg_precision precision, int* radices,
+                                       int* npass, int* first_group) {
+  if (!radices || !npass || !first_group) return fail(LFG_ERR_INVALID, "null output");
+  if (precision != LFG_F64 && precision != LFG_F32) return fail(LFG_ERR_INVALID, "bad precision");
+  if (n < 2 || n > ((size_t)1 << 24)) return fail(LFG_ERR_UNSUPPORTED, "size outside 2..2^24");
+  if (!smooth13((int64_t)n))
+    return fail(LFG_ERR_UNSUPPORTED, "sizes with a prime factor above 13 take the generic engine");
+  std::vector<int> rs = lfg::choose_radices((int64_t)n, precision);
+  const int64_t single = precision == 0 ? single_max_default() : lfg::kF32SingleGroupMax;
+  const int split = lfg::choose_split((int64_t)n, rs, single, precision, true);
+  if (split < 0 || (int)rs.size() > lfg::kMaxPass)
+    return fail(LFG_ERR_UNSUPPORTED, "no two-group split for this size");
+  std::copy(rs.begin(), rs.end(), radices);
+  *npass = (int)rs.size();
+  *first_group = split;
+  return LFG_OK;
+}
+
 static lfg_status lfg_wisdom_import_impl(const char* path) {
   if (!path) return fail(LFG_ERR_INVALID, "null path");
   if (!lfg::wisdom_import(path)) return fail(LFG_ERR_INVALID, std::string("cannot read ") + path);
@@ -1439,6 +1457,11 @@ lfg_status lfg_get_ragged_radices(const lfg_ragged* plan, int64_t n, int* radice
 
 lfg_status lfg_cos_sin_table(uint64_t n, double* out) {
   return guarded([&] { return lfg_cos_sin_table_impl(n, out); });
+}
+
+lfg_status lfg_plan_layout(size_t n, lfg_precision precision, int* radices, int* npass,
+                           int* first_group) {
+  return guarded([&] { return lfg_plan_layout_impl(n, precision, radices, npass, first_group); });
 }
 
 lfg_status lfg_wisdom_import(const char* path) {

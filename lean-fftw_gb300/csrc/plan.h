@@ -139,6 +139,11 @@ std::vector<int> choose_radices(int64_t n, int precision);
 // The fewest-operation radices of each factor of the most balanced split n = P * Q (larger
 // factor first), so split_point cuts at P; empty if n is prime or not 13-smooth.
 std::vector<int> balanced_radices(int64_t n);
+// Pass-group split of radix sequence rs for size N (the number of passes in the first group;
+// rs.size() = one group; -1 = no split of at most two groups fits): groups of at most
+// single_max points (0 = the shared-memory limit), then up to the shared-memory limit, then, if
+// may_reorder, after reordering rs around the most balanced factor pair (rs is updated).
+int choose_split(int64_t N, std::vector<int>& rs, int64_t single_max, int prec, bool may_reorder);
 // Largest binary32 size run as one pass group by default.  Binary32 is bound by HBM, and a
 // one-group tile above this size leaves one CTA per SM; larger sizes run two groups of about
 // sqrt(n) points each (choose_radices orders the radices for that split).

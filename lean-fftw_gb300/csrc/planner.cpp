@@ -352,21 +352,16 @@ std::vector<double> split_compensated(PassTables& pt, const std::vector<int>& rs
   return out;
 }
 
-std::string build_c2c(Plan& p, int64_t tile_target) {
-  const int64_t N = p.n;
-  const int prec = p.precision;
-  std::vector<int>& rs = p.radices;
-  std::string msg = check_radices(N, rs);
-  if (!msg.empty()) return msg;
+int choose_split(int64_t N, std::vector<int>& rs, int64_t single_max, int prec, bool may_reorder) {
   // pass grouping: one group when a transform fits one CTA's shared memory, else split the
   // sequence after the prefix whose product P best balances P against N/P
-  const int64_t single = p.single_max > 0 ? std::min(p.single_max, max_single_group(prec))
-                                          : max_single_group(prec);
+  const int64_t single = single_max > 0 ? std::min(single_max, max_single_group(prec))
+                                        : max_single_group(prec);
   int split = split_point(N, rs, single);
   // no split within the preferred group size: allow groups up to the shared-memory limit, and
   // (for a planner-chosen order) reorder the radices around the most balanced factor pair
   if (split < 0) split = split_point(N, rs, max_single_group(prec));
-  if (split < 0 && !p.radices_given) {
+  if (split < 0 && may_reorder) {
     std::vector<int> bal = balanced_radices(N);
     const int s2 = bal.empty() ? -1 : split_point(N, bal, max_single_group(prec));
     if (s2 >= 0) {
@@ -374,6 +369,16 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
       split = s2;
     }
   }
+  return split;
+}
+
+std::string build_c2c(Plan& p, int64_t tile_target) {
+  const int64_t N = p.n;
+  const int prec = p.precision;
+  std::vector<int>& rs = p.radices;
+  std::string msg = check_radices(N, rs);
+  if (!msg.empty()) return msg;
+  const int split = choose_split(N, rs, p.single_max, prec, !p.radices_given);
   if (split < 0) return "size too large for two pass groups with this radix order";
   PassTables pt = make_pass_tables(N, p.fwd, rs, prec);
   const std::vector<int> comp = compensated_passes(N, rs, split, p.no_comp ? 0 : prec);

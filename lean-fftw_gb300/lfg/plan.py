@@ -198,3 +198,13 @@ def wisdom_forget() -> None:
 def wisdom_count() -> int:
     """Entries held in the process's tuning cache (lfg_wisdom_count)."""
     return int(lib().lfg_wisdom_count())
+
+
+def plan_layout(n: int, precision="f64"):
+    """(radices, passes in the first pass group) of a default 1-D plan of size n, computed on
+    the host (lfg_plan_layout); the first group holds every pass when the plan has one group."""
+    rs = (ctypes.c_int * 24)()
+    npass, first = ctypes.c_int(), ctypes.c_int()
+    check(lib().lfg_plan_layout(int(n), _prec(precision), rs, ctypes.byref(npass),
+                                ctypes.byref(first)))
+    return [rs[i] for i in range(npass.value)], first.value
