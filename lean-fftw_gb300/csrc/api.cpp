@@ -823,19 +823,7 @@ lfg_status plan_rdft2_packed(bool r2c, const std::vector<SDim>& T, const std::ve
   return wrap_plan(p, out);
 }
 
-// Runs an entry point's body, turning C++ exceptions into statuses.
-template <class F>
-lfg_status guarded(F&& body) {
-  try {
-    return body();
-  } catch (const std::bad_alloc&) {
-    return fail(LFG_ERR_NOMEM, "host allocation failed");
-  } catch (const std::exception& e) {
-    return fail(LFG_ERR_INVALID, std::string("internal error: ") + e.what());
-  } catch (...) {
-    return fail(LFG_ERR_INVALID, "internal error");
-  }
-}
+using lfg::guarded;
 
 }  // namespace
 

@@ -55,34 +55,7 @@ cudaError_t static_scratch(void** out) {
   return cudaSuccess;
 }
 
-// The two-group launch sequence of an in-place complex plan with a caller-given intermediate
-// (contiguous lines of n elements); single-group plans need none.
-cudaError_t run_inplace(const lfg::Plan& p, void* data, void* scratch, cudaStream_t stream) {
-  const size_t es = p.precision == 0 ? 16 : 8;
-  char* base = static_cast<char*>(data);
-  const char* ib = base + p.in.offset * (int64_t)es;
-  char* ob = base + p.out.offset * (int64_t)es;
-  auto launch = [&](const lfg::GroupDesc& g, const void* a, void* b) -> cudaError_t {
-    if (p.precision == 0) return lfg::launch_group_f64(g, p.fwd, a, b, stream);
-    return lfg::launch_group_f32(g, p.fwd, a, b, stream);
-  };
-  if (p.ngroups == 1) return launch(p.groups[0], ib, ob);
-  lfg::GroupDesc g1 = p.groups[0], g2 = p.groups[1];
-  const int64_t P = g2.nsub;
-  g1.out_line = p.n;
-  g1.out_sub = P;
-  g1.out_elem = 1;
-  g2.in_line = p.n;
-  g2.in_sub = 1;
-  g2.in_elem = P;
-  cudaError_t e = launch(g1, ib, scratch);
-  if (e != cudaSuccess) return e;
-  return launch(g2, scratch, ob);
-}
-
-}  // namespace
-
-extern "C" lfg_status lfg_execute_inplace_static(const lfg_plan* plan, void* data, void* stream) {
+lfg_status execute_inplace_static(const lfg_plan* plan, void* data, void* stream) {
   if (!plan || !data) {
     lfg::set_last_error("null plan or buffer");
     return LFG_ERR_INVALID;
@@ -93,13 +66,21 @@ extern "C" lfg_status lfg_execute_inplace_static(const lfg_plan* plan, void* dat
     return LFG_ERR_UNSUPPORTED;
   }
   if (p.empty) return LFG_OK;
-  if ((uintptr_t)data & (p.precision == 0 ? 15u : 7u)) {
-    lfg::set_last_error("buffer must be aligned to a complex element (16 bytes binary64, 8 bytes binary32)");
-    return LFG_ERR_INVALID;
+  // only plans that run as one or two pass groups of the Stockham kernels: sizes with a prime
+  // factor above 13 (generic-engine and Bluestein plans) and dense-buffer plans (split arrays,
+  // negative strides) keep buffers of their own and are refused before anything runs
+  if (p.generic || p.chirp_fwd || !p.steps.empty() || (p.ngroups != 1 && p.ngroups != 2)) {
+    lfg::set_last_error("static-scratch execution takes 13-smooth sizes in one or two pass "
+                        "groups only (this plan runs another algorithm)");
+    return LFG_ERR_UNSUPPORTED;
   }
   if (!p.stages.empty() || p.howmany2 > 1) {
     lfg::set_last_error("static-scratch execution takes 1-D plans with one batch dimension");
     return LFG_ERR_UNSUPPORTED;
+  }
+  if ((uintptr_t)data & (p.precision == 0 ? 15u : 7u)) {
+    lfg::set_last_error("buffer must be aligned to a complex element (16 bytes binary64, 8 bytes binary32)");
+    return LFG_ERR_INVALID;
   }
   const size_t es = p.precision == 0 ? 16 : 8;
   const size_t need = (size_t)p.n * (size_t)p.howmany * es;
@@ -110,10 +91,19 @@ extern "C" lfg_status lfg_execute_inplace_static(const lfg_plan* plan, void* dat
   }
   void* scratch = nullptr;
   cudaError_t e = p.ngroups == 2 ? static_scratch(&scratch) : cudaSuccess;
-  if (e == cudaSuccess) e = run_inplace(p, data, scratch, static_cast<cudaStream_t>(stream));
+  // the regular launch sequence, in place, with the static array as the two-group
+  // intermediate (a one-group plan needs none)
+  if (e == cudaSuccess)
+    e = lfg::execute_plan(p, data, data, static_cast<cudaStream_t>(stream), false, scratch);
   if (e != cudaSuccess) {
     lfg::set_last_error(std::string("static-scratch execution: ") + cudaGetErrorString(e));
     return LFG_ERR_CUDA;
   }
   return LFG_OK;
+}
+
+}  // namespace
+
+extern "C" lfg_status lfg_execute_inplace_static(const lfg_plan* plan, void* data, void* stream) {
+  return lfg::guarded([&] { return execute_inplace_static(plan, data, stream); });
 }

@@ -192,7 +192,10 @@ void free_plan_memory(Plan& p);
 
 // force_scratch: keep the intermediate of two-group plans in the plan's device scratch even
 // out of place (used when `out` is host memory mapped into the device's address space).
+// scratch: a caller-supplied device buffer of n * howmany complex elements that takes the
+// place of the plan's own scratch for the intermediate of a one-block two-group plan (the
+// plan's scratch is then neither allocated nor touched); nullptr = the plan's own.
 cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream,
-                         bool force_scratch = false);
+                         bool force_scratch = false, void* scratch = nullptr);
 
 }  // namespace lfg

@@ -618,7 +618,7 @@ static cudaError_t ensure_scratch(const Plan& p) {
 }
 
 cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t stream,
-                         bool force_scratch) {
+                         bool force_scratch, void* scratch) {
   if (p.empty) return cudaSuccess;
   if (p.generic) {
     const size_t ces = p.precision == 0 ? 16 : 8;
@@ -753,9 +753,11 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     z_line = p.out.dist;
     z_stride = p.out.stride;
   } else {
-    cudaError_t e = ensure_scratch(p);
-    if (e != cudaSuccess) return e;
-    zb = static_cast<char*>(p.d_scratch);
+    if (!scratch) {
+      cudaError_t e = ensure_scratch(p);
+      if (e != cudaSuccess) return e;
+    }
+    zb = static_cast<char*>(scratch ? scratch : p.d_scratch);
     z_line = p.n;
     z_stride = 1;
   }

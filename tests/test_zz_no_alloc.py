@@ -5,8 +5,9 @@ memory through their own pool, or loops that cannot take cudaMalloc's implicit d
 synchronisation), the library offers this one entry point: a two-group plan's intermediate
 goes to a fixed 16 MiB static device array instead of a cudaMalloc'd plan buffer.  Called
 through the C ABI with ctypes, its output must equal the regular entry point's (lfg_execute,
-in place), bit for bit -- the tolerance every parity test here uses -- on two calls in a row;
-and a plan whose intermediate would not fit the array is refused with a clear error.
+in place), bit for bit -- the tolerance every parity test here uses -- on two calls in a row,
+in binary64 and binary32, one pass group and two; a plan whose intermediate would not fit the
+array, or that runs another algorithm (a prime factor above 13), is refused with a clear error.
 
 This file sorts last on purpose, so a run that stops at the first failure has run every other
 test first; it also passes alone in a fresh process.
@@ -39,11 +40,13 @@ def _random(shape, dtype, seed):
     return torch.view_as_complex(real).to(dtype).cuda()
 
 
-@pytest.mark.parametrize("n,howmany,precision", [(16384, 32, "f64"), (65536, 8, "f64"),
-                                                 (8192, 64, "f32"), (1024, 16, "f64")])
-def test_static_scratch_matches_regular_entry(n, howmany, precision):
+@pytest.mark.parametrize("n,howmany,precision,groups", [
+    (16384, 32, "f64", 2), (65536, 8, "f64", 2), (1024, 16, "f64", 1),
+    (8192, 64, "f32", 1), (16384, 32, "f32", 2), (65536, 16, "f32", 2)])
+def test_static_scratch_matches_regular_entry(n, howmany, precision, groups):
     dtype = torch.complex128 if precision == "f64" else torch.complex64
     plan = lfg.plan_1d(n, -1, howmany, precision=precision)
+    assert plan.info().ngroups == groups           # two-group plans use the static array
     stream = torch.cuda.current_stream().cuda_stream
     f = _entry()
     for call in range(2):                           # two calls in a row share the array
@@ -69,3 +72,18 @@ def test_oversized_intermediate_is_refused():
     assert b"static scratch" in lfg.lib().lfg_last_error()
     torch.cuda.synchronize()
     assert torch.equal(buf, before)                 # nothing ran
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_other_algorithms_are_refused(precision):
+    """n = 17 runs the generic engine's sums (binary64) or Bluestein's convolution (binary32),
+    which keep buffers of their own: refused on the host before anything is launched."""
+    plan = lfg.plan_1d(17, -1, 4, precision=precision)
+    dtype = torch.complex128 if precision == "f64" else torch.complex64
+    buf = _random((4, 17), dtype, seed=17)
+    before = buf.clone()
+    rc = _entry()(ctypes.c_void_p(plan.handle), ctypes.c_void_p(buf.data_ptr()), None)
+    assert rc == LFG_ERR_UNSUPPORTED
+    assert b"13-smooth" in lfg.lib().lfg_last_error()
+    torch.cuda.synchronize()
+    assert torch.equal(buf, before)
