@@ -18,10 +18,13 @@ What is here, and the reference code each piece follows (paths inside lean-fftw)
                        `dd_r2r` (extended precision).
 * `dd_dft`             extended-precision (double-double) DFT: the accuracy oracle.
 * `lcg_rand`           randArr of scripts/AsmTest.lean:7-13, the reference tests' inputs.
+* `bfly`               one butterfly of the oracle: radices 2, 4, 8 and 16 are lean-fftw's own
+                       generated kernels (LeanFFTW/Native/Kernels.lean, via native_dag.py).
 
 The reference engine itself cannot run here: it needs a Lean 4.35 toolchain (absent, no
 network) and AVX-512 (absent on aarch64 hosts).  Parity is pinned instead through the
-reference's published known answers (see tests/test_oracle_pins.py).
+reference's published known answers and generated kernels (tests/test_oracle.py,
+tests/test_codegen_pins.py, tests/test_native_kernels.py).
 
 Only tests, the smoke check and the CPU-baseline leg of the benchmark may import this module.
 """
@@ -70,12 +73,26 @@ def lib() -> ctypes.CDLL:
     L.lfo_rel_l2.restype = ctypes.c_double
     L.lfo_cos_sin_table.argtypes = [ctypes.c_uint64, _dp]
     L.lfo_cos_sin_table.restype = ctypes.c_int
+    L.lfo_bfly.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp]
+    L.lfo_bfly.restype = ctypes.c_int
     return L
 
 
 def _p(a: np.ndarray):
     assert a.flags.c_contiguous
     return a.ctypes.data_as(_dp)
+
+
+def bfly(fwd: bool, R: int, tw: bool, x: np.ndarray, native: bool = True) -> np.ndarray:
+    """One radix-R butterfly of the oracle on x (2R data values, then 2(R-1) twiddle values
+    when tw): lean-fftw's generated kernel (native, radices 2/4/8/16) or the restated
+    generator's (other radices)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    assert x.size == (4 * R - 2 if tw else 2 * R)
+    y = np.empty(2 * R, dtype=np.float64)
+    if lib().lfo_bfly(int(fwd), R, int(tw), int(native), _p(x), _p(y)) != 0:
+        raise ValueError(f"no oracle butterfly for radix {R}")
+    return y
 
 
 def nthreads_default() -> int:

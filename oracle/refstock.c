@@ -4,9 +4,11 @@
  *
  *  1. lfo_ref_transform: `refTransform` / `stockhamWith floatArith` / `passWith` /
  *     `bflyInputs` (LeanFFTW/Gen/Stockham.lean:263-301), the binary64 reference that
- *     lean-fftw's fast engine reproduces bit for bit.  The butterfly kernels come from the
- *     generated file codelets_ref.c (restated codelet generator, evaluated operand for
- *     operand with fma(); this file must be compiled with -ffp-contract=off).
+ *     lean-fftw's fast engine reproduces bit for bit.  The butterfly kernels of radix 2, 4,
+ *     8 and 16 are lean-fftw's own generated kernels (codelets_native.c, written from
+ *     LeanFFTW/Native/Kernels.lean); the other radices come from the restated codelet
+ *     generator (codelets_gen.c).  Both are evaluated operand for operand with fma(); this
+ *     file must be compiled with -ffp-contract=off.
  *  2. lfo_generic_dft: the generic engine, `exec floatOps (mkPlan floatOps fwd
  *     (primeFactors n))` (LeanFFTW/Core/Alg.lean:236-254, Core/FloatOps.lean:52-68,
  *     Core/Problem.lean:126-127), which lean-fftw runs for r2c/c2r and rank >= 2.
@@ -26,8 +28,33 @@
 
 typedef void (*lfo_codelet_fn)(const double *x, double *y);
 typedef void (*lfo_pass_fn)(long N, long ns, const double *tw, const double *z, double *o);
-lfo_codelet_fn lfo_codelet(int fwd, int R, int tw);
-lfo_pass_fn lfo_pass(int fwd, int R, int tw);
+lfo_codelet_fn lfo_native_codelet(int fwd, int R, int tw);
+lfo_pass_fn lfo_native_pass(int fwd, int R, int tw);
+lfo_codelet_fn lfo_codelet_gen(int fwd, int R, int tw);
+lfo_pass_fn lfo_pass_gen(int fwd, int R, int tw);
+
+/* The butterfly of radix R: lean-fftw's generated kernel where it ships one, else the
+ * restated generator's. */
+lfo_codelet_fn lfo_codelet(int fwd, int R, int tw)
+{
+     lfo_codelet_fn f = lfo_native_codelet(fwd, R, tw);
+     return f ? f : lfo_codelet_gen(fwd, R, tw);
+}
+
+static lfo_pass_fn lfo_pass(int fwd, int R, int tw)
+{
+     lfo_pass_fn f = lfo_native_pass(fwd, R, tw);
+     return f ? f : lfo_pass_gen(fwd, R, tw);
+}
+
+/* Evaluate one butterfly (x: 2R data values, then 2(R-1) twiddle values when tw; y: 2R). */
+int lfo_bfly(int fwd, int R, int tw, int native, const double *x, double *y)
+{
+     lfo_codelet_fn f = native ? lfo_native_codelet(fwd, R, tw) : lfo_codelet_gen(fwd, R, tw);
+     if (!f) return -1;
+     f(x, y);
+     return 0;
+}
 
 /* ------------------------------------------------------------------ 1. refTransform */
 

@@ -1,12 +1,12 @@
 """Regenerate the committed golden fixtures under tests/golden/.
 
-    python tests/golden/make_golden.py [--reference DIR]
+    python tests/golden/make_golden.py --reference DIR     (or LEAN_FFTW_REFERENCE=DIR)
 
 Two kinds of fixture:
 
-1. Known answers published by lean-fftw (read from a checkout of the reference; the
-   default path is where this build's container mounts it).  They are copied verbatim or
-   re-encoded as JSON, never re-derived:
+1. Known answers published by lean-fftw (read from a checkout of the reference given by
+   --reference or the LEAN_FFTW_REFERENCE variable; without one only the oracle vectors are
+   rewritten).  They are copied verbatim or re-encoded as JSON, never re-derived:
      kernel_constants.txt  results/repro-2026-11-04/kernel-constants.txt (237 binary64
                            bit patterns of every codelet constant, radix <= 64)
      bounds.jsonl          results/repro-2026-11-04/bounds.jsonl (rounding depth a,
@@ -14,6 +14,9 @@ Two kinds of fixture:
      xcheck.json           results/repro-2026-11-04/xcheck-bits.jsonl (chosen plan and
                            relative L2 error against long-double FFTW, 36 sizes)
      opcounts.json         docs/ITERATIONS.md:227-230 and :285-287 (kernel op counts)
+     native_kernels.json   LeanFFTW/Native/Kernels.lean:9-1897 (the sixteen generated
+                           radix-2/4/8/16 butterflies, parsed by oracle/native_dag.py into
+                           operation lists with their constant bits)
 2. Input/output vectors of the CPU oracle (oracle/oracle.py, refTransform restated) on the
    reference tests' own LCG inputs (scripts/AsmTest.lean:7-13): oracle_vectors.npz.
 """
@@ -68,6 +71,20 @@ def copy_reference_pins(ref: str) -> None:
         json.dump({"split": counts, "untwiddled_totals": totals,
                    "twiddled8_total": int(m8.group(1)),
                    "source": "lean-fftw docs/ITERATIONS.md:61-62, 227-230, 285-287"}, f, indent=1)
+    native_kernels(ref)
+
+
+def native_kernels(ref: str) -> None:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import native_dag
+    text = open(os.path.join(ref, native_dag.SOURCE)).read()
+    ks = native_dag.parse_lean(text)
+    with open(native_dag.FIXTURE, "w") as f:
+        f.write('{"source": "lean-fftw ' + native_dag.SOURCE + '",\n "kernels": {\n')
+        rows = []
+        for name in sorted(ks, key=lambda n: (ks[n]["R"], ks[n]["tw"], not ks[n]["fwd"])):
+            rows.append(f'  "{name}": ' + json.dumps(ks[name], separators=(",", ":")))
+        f.write(",\n".join(rows) + "\n}}\n")
 
 
 def oracle_vectors() -> None:
@@ -85,9 +102,14 @@ def oracle_vectors() -> None:
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("LEAN_FFTW_REFERENCE"),
+                    help="checkout of lean-fftw (default: $LEAN_FFTW_REFERENCE)")
     a = ap.parse_args()
-    if os.path.isdir(a.reference):
+    if a.reference:
+        if not os.path.isdir(a.reference):
+            sys.exit(f"make_golden: {a.reference} is not a directory")
         copy_reference_pins(a.reference)
+    else:
+        print("make_golden: no reference checkout given; published pins left as they are")
     oracle_vectors()
     print("golden fixtures written to", HERE)
