@@ -76,29 +76,111 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def figures():
+    """Figures measured outside the timed run (profiles/figures.json): the DFMA issue rate
+    (`--workload fp64_peak`) and the ncu DRAM traffic of each workload's dominant kernel."""
+    p = os.path.join(ROOT, "profiles", "figures.json")
+    return json.load(open(p)) if os.path.exists(p) else {}
+
+
 def fp64_peak():
-    """DFMA issue rate measured on this machine's GB300 (profiles/fp64_issue_rate.md)."""
-    p = os.path.join(ROOT, "profiles", "fp64_issue_rate.md")
-    if os.path.exists(p):
-        for line in open(p):
-            if line.startswith("dfma_tinstr_per_s:"):
-                return float(line.split(":")[1])
-    return None
-
-
-PROFILE_OF = {"ragged": "ragged_kernel_f64_ragged8192.md",
-              "c2c_1024": "group_kernel_f64_c2c1024.md",
-              "c2c_1024_f32": "stream_kernel_f32_c2c1024.md"}
+    """DFMA issue rate of a GB300 in T instructions/s (the binding roofline of binary64)."""
+    return figures().get("fp64_issue", {}).get("dfma_tinstr_per_s")
 
 
 def ncu_traffic(workload):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", PROFILE_OF.get(workload, "-"))
-    if os.path.exists(p):
-        for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
-    return None
+    """DRAM bytes per launch of the dominant kernel, from its committed ncu capture."""
+    t = figures().get("traffic", {}).get(workload)
+    return float(t["bytes_per_launch"]) if t else None
+
+
+# Issue-rate probe of the FP64 pipe: every warp runs 8 independent chains of one binary64
+# instruction form over operands read from device memory (so the compiler cannot fold the
+# fused forms back into an add or a multiply); 8 CTAs of 256 threads per SM.
+FP64_PROBE_SRC = r"""
+#include <cuda_runtime.h>
+template <int OP>
+__global__ void __launch_bounds__(256) chains(double* out, const double* p, int iters) {
+  const double one = p[0], c = p[1], m = p[2], nz = p[3];
+  double v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = (double)(threadIdx.x + i) * 1e-3;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (OP == 0) v[i] = __dadd_rn(v[i], c);
+      if (OP == 1) v[i] = __fma_rn(v[i], one, c);
+      if (OP == 2) v[i] = __fma_rn(v[i], m, c);
+      if (OP == 3) v[i] = __dmul_rn(v[i], m);
+      if (OP == 4) v[i] = __fma_rn(v[i], m, nz);
+    }
+  }
+  double s = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += v[i];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+template <int OP>
+static float time_op(double* out, const double* p, int grid, int iters) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  chains<OP><<<grid, 256>>>(out, p, iters);
+  cudaEventRecord(a);
+  for (int r = 0; r < 5; ++r) chains<OP><<<grid, 256>>>(out, p, iters);
+  cudaEventRecord(b);
+  cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / 5;
+}
+// rates[0..4]: T instr/s of DADD, DFMA(x,1,c), DFMA(x,m,c), DMUL, DFMA(x,m,-0)
+extern "C" int lfg_fp64_probe(double* rates) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) return -1;
+  const int grid = sms * 8, iters = 4096;
+  double *out = nullptr, *p = nullptr;
+  if (cudaMalloc(&out, (size_t)grid * 256 * sizeof(double)) != cudaSuccess) return -1;
+  if (cudaMalloc(&p, 4 * sizeof(double)) != cudaSuccess) return -1;
+  const double h[4] = {1.0, 1e-9, 1.0000001, -0.0};
+  cudaMemcpy(p, h, sizeof h, cudaMemcpyHostToDevice);
+  const double ops = (double)grid * 256 * 8 * iters;
+  const float t[5] = {time_op<0>(out, p, grid, iters), time_op<1>(out, p, grid, iters),
+                      time_op<2>(out, p, grid, iters), time_op<3>(out, p, grid, iters),
+                      time_op<4>(out, p, grid, iters)};
+  for (int i = 0; i < 5; ++i) rates[i] = ops / (t[i] * 1e-3) / 1e12;
+  cudaFree(out);
+  cudaFree(p);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+"""
+
+
+def run_fp64_peak(args):
+    """`--workload fp64_peak`: the FP64 pipe's issue rates on this GPU (one JSON line)."""
+    import ctypes
+    import tempfile
+    from lfg.build import ARCH, nvcc
+    with tempfile.TemporaryDirectory() as d:
+        src, so = os.path.join(d, "probe.cu"), os.path.join(d, "probe.so")
+        open(src, "w").write(FP64_PROBE_SRC)
+        subprocess.run([nvcc(), *ARCH, "-O3", "-shared", "-Xcompiler", "-fPIC", src, "-o", so],
+                       check=True)
+        lib = ctypes.CDLL(so)
+        rates = (ctypes.c_double * 5)()
+        with Clocks(0) as clk:
+            rc = lib.lfg_fp64_probe(rates)
+    if rc != 0:
+        raise SystemExit("fp64_peak: the probe failed")
+    names = ["dadd", "dfma_one", "dfma", "dmul", "dfma_nz"]
+    line = {"metric": "FP64 issue rate (T instr/s)", "value": round(rates[2], 4),
+            "unit": "T instr/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+            "config": {"workload": "fp64_peak", "grid": "8 CTAs x 256 threads per SM",
+                       "chains_per_thread": 8, "iterations": 4096},
+            "rates": {k: round(v, 4) for k, v in zip(names, rates)}, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
 
 
 class Clocks:
@@ -183,9 +265,10 @@ def rank_seed(rank):
     return SEED + rank
 
 
-def cpu_reference(wl, steps, warmup, budget_s=None):
+def cpu_reference(wl, runs=10, budget_s=None):
     """Time the oracle's restatement of refTransform on all host threads (one transform per
-    thread) on a bounded sample of the workload; returns (GFLOP/s, threads, sample text)."""
+    thread) on a bounded sample of the workload, by libbench2's protocol; returns a dict with
+    GFLOP/s, threads, a description of the sample and the published engine's figures."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle as O
@@ -201,6 +284,7 @@ def cpu_reference(wl, steps, warmup, budget_s=None):
         flops = float(sum(flops_per_transform(int(n)) for n in sizes))
         sample = f"the whole batch ({len(sizes)} transforms, {len(plans)} sizes) per timed call"
     elif wl["kind"] == "r2c2d":
+        sizes = None
         # lean-fftw runs rdft2 in its generic engine (Core/Problem.lean:222-236): restated
         n0, n1 = wl["n0"], wl["n1"]
         count = min(wl["batch"], max(1, threads // 2))
@@ -210,6 +294,7 @@ def cpu_reference(wl, steps, warmup, budget_s=None):
         sample = (f"{count} of the {wl['batch']} images ({n0}x{n1}, binary64) per timed call "
                   "through the generic engine's rdft2")
     else:
+        sizes = None
         n = wl["n"]
         rs = reference_plan(n)
         count = max(threads, min(wl["batch"], threads * max(1, (1 << 15) // n)))
@@ -217,18 +302,75 @@ def cpu_reference(wl, steps, warmup, budget_s=None):
         call = lambda: O.ref_transform(wl["sign"] < 0, n, rs, x, nthreads=threads)
         flops = flops_per_transform(n) * count
         sample = f"{count} of the {wl['batch']} transforms of N={n} (plan {'x'.join(map(str, rs))}) per timed call"
+    t, runs = libbench2_time(call, runs=runs, budget_s=budget_s)
+    out = {"gflops": flops / t / 1e9, "threads": threads,
+           "sample": sample + f"; libbench2 protocol: iterations doubled to >= 10 ms, best of 8, "
+                              f"median of {runs} runs"}
+    pub = published_engine(wl, sizes if wl["kind"] == "ragged" else None)
+    if pub:
+        out["published"] = pub
+    return out
+
+
+def libbench2_time(call, runs=10, budget_s=None):
+    """Seconds per call by libbench2's protocol (lean-fftw docs/BENCHMARK_PROTOCOL.md:15-19,
+    33-37): the iteration count doubles until one measurement takes at least 10 ms; a run is
+    the best of 8 measurements; the result is the median of `runs` runs (fewer if `budget_s`
+    of measuring is spent).  Returns (seconds per call, runs done)."""
     call()
-    for _ in range(warmup):
-        call()
-    times = []
-    for _ in range(max(1, steps)):
+    iters = 1
+    while True:
         t0 = time.perf_counter()
-        call()
-        times.append(time.perf_counter() - t0)
-        if budget_s and sum(times) > budget_s:
+        for _ in range(iters):
+            call()
+        if time.perf_counter() - t0 >= 0.01:
             break
-    t = statistics.median(times)
-    return flops / t / 1e9, threads, sample + f", median of {len(times)}"
+        iters *= 2
+    per_run, start = [], time.perf_counter()
+    for _ in range(runs):
+        best = math.inf
+        for _ in range(8):
+            t0 = time.perf_counter()
+            for _ in range(iters):
+                call()
+            best = min(best, (time.perf_counter() - t0) / iters)
+        per_run.append(best)
+        if budget_s and time.perf_counter() - start > budget_s:
+            break
+    return statistics.median(per_run), len(per_run)
+
+
+def published_engine(wl, sizes=None):
+    """lean-fftw's published engine on one core (docs/RESULTS.md:72-89, i12 on Emerald Rapids,
+    AVX-512; it cannot run on this host): GFLOP/s per core at N = 1024 and, for the workload,
+    the single-core rate its per-size medians imply (log-linear interpolation in log2 N
+    between the published power-of-two sizes; non-power-of-two sizes are an estimate)."""
+    p = os.path.join(ROOT, "tests", "golden", "published_times.json")
+    if not os.path.exists(p):
+        return None
+    tab = {int(k): v["i12_s"] for k, v in json.load(open(p))["times"].items()}
+    ks = sorted(tab)
+    rate = {n: flops_per_transform(n) / tab[n] / 1e9 for n in ks}
+
+    def core_rate(n):
+        if n <= ks[0]:
+            return rate[ks[0]]
+        if n >= ks[-1]:
+            return rate[ks[-1]]
+        hi = next(k for k in ks if k >= n)
+        lo = ks[ks.index(hi) - 1]
+        f = (math.log2(n) - math.log2(lo)) / (math.log2(hi) - math.log2(lo))
+        return rate[lo] + f * (rate[hi] - rate[lo])
+
+    out = {"engine": "lean-fftw i12, one Emerald Rapids core (AVX-512), published medians",
+           "source": "docs/RESULTS.md:72-89", "core_gflops_n1024": round(rate[1024], 2)}
+    if sizes is not None:
+        t = sum(flops_per_transform(int(n)) / core_rate(int(n)) for n in sizes)
+        out["core_gflops_workload_estimate"] = round(
+            sum(flops_per_transform(int(n)) for n in sizes) / t, 2)
+    elif wl.get("n"):
+        out["core_gflops_workload_estimate"] = round(core_rate(wl["n"]), 2)
+    return out
 
 
 def ragged_workload_sizes(wl):
@@ -270,19 +412,125 @@ def workload_config(name, wl):
     return {"workload": name, "n": wl["n"], "batch": wl["batch"], "sign": wl["sign"]}
 
 
+def ragged_accuracy(sizes, host, out, count=64):
+    """"At ref error" for the ragged batch: a sample of `count` transforms spread over the
+    sizes (evenly in size order) against the double-double DFT, beside lean-fftw's reference
+    transform of the same inputs (the oracle's refTransform, reference plans): aggregate
+    relative L2 over the sample for both, their ratio, and the worst per-transform ratio."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    pick = np.unique(np.linspace(0, len(sizes) - 1, count).round().astype(np.int64))
+    e_gpu = e_ref = den = 0.0
+    worst = 0.0
+    for i in pick:
+        n, a = int(sizes[i]), int(off[i])
+        x = np.ascontiguousarray(host[a:a + n])[None]
+        hi, lo = O.dd_dft(True, x)
+        norm2 = float(np.sum(np.abs(hi) ** 2))
+        eg = O.rel_l2(np.ascontiguousarray(out[a:a + n]), (hi[0], lo[0]))
+        er = O.rel_l2(O.ref_transform(True, n, reference_plan(n), x)[0], (hi[0], lo[0]))
+        e_gpu += eg * eg * norm2
+        e_ref += er * er * norm2
+        den += norm2
+        if er > 0:
+            worst = max(worst, eg / er)
+    l2, rl2 = math.sqrt(e_gpu / den), math.sqrt(e_ref / den)
+    return {"sample": f"{len(pick)} transforms, evenly spaced in size order "
+                      f"(N = {int(sizes[pick[0]])} .. {int(sizes[pick[-1]])})",
+            "oracle": "double-double DFT", "l2_err": float(f"{l2:.4g}"),
+            "ref_l2_err": float(f"{rl2:.4g}"), "ratio": round(l2 / rl2, 4),
+            "worst_transform_ratio": round(worst, 4), "bar": 1.5}
+
+
+def published_accuracy():
+    """lean-fftw's published forward/backward relative L2 errors per power-of-two size
+    (results/emr-i12/accuracy.txt, committed as tests/golden/accuracy_emr.json)."""
+    p = os.path.join(ROOT, "tests", "golden", "accuracy_emr.json")
+    return {int(k): v for k, v in json.load(open(p))["errors"].items()} if os.path.exists(p) else {}
+
+
+def run_precision(args):
+    """`--workload precision`: relative L2 error per size against the double-double DFT, for
+    the binary64 path, the binary32 path (compensated last-pass twiddles from 2^16, and plain
+    products), lean-fftw's reference transform (the oracle's refTransform with the reference's
+    plans) and the reference's published errors: c2c N = 2^k (k = 1..18; 32 transforms of
+    2^18, as in the large-N configuration) and 64 real 512 x 512 images (rdft2)."""
+    import numpy as np
+    import torch
+
+    import lfg
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    torch.cuda.set_device(0)
+    threads = os.cpu_count() or 1
+    pub = published_accuracy()
+    rows = []
+    t0 = time.perf_counter()
+    for k in range(1, 19):
+        n = 1 << k
+        B = 32 if k == 18 else max(1, min(64, (1 << 20) // n))
+        x = O.uniform_complex((B, n), seed=SEED + k)
+        x32 = x.astype(np.complex64)
+        row = {"n": n, "batch": B}
+        for fwd in (True, False):
+            d = "fwd" if fwd else "bwd"
+            ref = O.dd_dft(fwd, x, nthreads=threads)
+            ref32 = O.dd_dft(fwd, x32.astype(np.complex128), nthreads=threads)
+            plan = lfg.plan_1d(n, -1 if fwd else 1, B)
+            y = plan.execute(torch.from_numpy(x).cuda()).cpu().numpy()
+            row[f"f64_{d}"] = O.rel_l2(y, ref)
+            r = O.ref_transform(fwd, n, reference_plan(n), x, nthreads=threads)
+            row[f"ref_{d}"] = O.rel_l2(r, ref)
+            for comp in ((True, False) if k >= 16 else (True,)):
+                p32 = lfg.plan_1d(n, -1 if fwd else 1, B, precision="f32", compensated=comp)
+                y32 = p32.execute(torch.from_numpy(x32).cuda()).cpu().numpy()
+                row[f"f32_{d}" if comp else f"f32_plain_{d}"] = O.rel_l2(y32.astype(np.complex128), ref32)
+            if n in pub:
+                row[f"published_{d}"] = pub[n][f"{d}_l2"]
+        row["ratio_f64_to_ref"] = max(row["f64_fwd"] / row["ref_fwd"] if row["ref_fwd"] else 1.0,
+                                      row["f64_bwd"] / row["ref_bwd"] if row["ref_bwd"] else 1.0)
+        rows.append({k2: (float(f"{v:.4g}") if isinstance(v, float) else v) for k2, v in row.items()})
+    # rank-2 real: 64 images of 512 x 512 (the generic engine is the reference's rdft2 path)
+    xi = np.random.default_rng(SEED).random((64, 512, 512)) - 0.5
+    ref = O.dd_rank2_r2c(xi, nthreads=threads)
+    img = {"shape": [512, 512], "batch": 64}
+    for prec in ("f64", "f32"):
+        xin = xi.astype(np.float32) if prec == "f32" else xi
+        refp = ref if prec == "f64" else O.dd_rank2_r2c(xin.astype(np.float64), nthreads=threads)
+        plan = lfg.plan_r2c_2d(512, 512, 64, precision=prec)
+        yd = torch.empty((64, 512, 257), device="cuda",
+                         dtype=torch.complex64 if prec == "f32" else torch.complex128)
+        y = plan.execute(torch.from_numpy(np.ascontiguousarray(xin)).cuda(), yd).cpu().numpy()
+        img[f"{prec}"] = float(f"{O.rel_l2(y.astype(np.complex128), refp):.4g}")
+    img["ref_generic"] = float(f"{O.rel_l2(O.generic_rank2_r2c(xi, nthreads=threads), ref):.4g}")
+    worst = max(r["ratio_f64_to_ref"] for r in rows)
+    line = {"metric": "relative L2 error vs double-double DFT, binary64 / reference (worst size)",
+            "value": round(worst, 4), "unit": "ratio", "n_gpus": 1, "higher_is_better": False,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "precision", "inputs": "re/im iid uniform[-0.5, 0.5), seed "
+                       "20261016 + log2 N", "oracle": "double-double DFT",
+                       "reference": "refTransform restated, reference plans"},
+            "c2c": rows, "r2c_512x512": img,
+            "wall_s": round(time.perf_counter() - t0, 1)}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, wl):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    gf, threads, sample = cpu_reference(wl, max(1, args.steps), max(0, min(args.warmup, 2)),
-                                        budget_s=60)
+    cb = cpu_reference(wl, runs=max(1, min(args.steps, 10)), budget_s=60)
+    gf, threads, sample = cb["gflops"], cb["threads"], cb["sample"]
     line = {"metric": metric_name(wl), "value": round(gf, 3),
             "unit": "GFLOP/s", "impl": "reference", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args.workload, wl),
             "cpu_baseline": {"value": round(gf, 3), "unit": "GFLOP/s", "cores": threads,
-                             "kind": "port", "sample": sample},
+                             "kind": "port", "sample": sample,
+                             "published": cb.get("published")},
             "e2e": {"value": round(gf, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -334,7 +582,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=600)   # ~1 s timed: several clock samples
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="ragged", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="ragged",
+                    choices=sorted(WORKLOADS) + ["fp64_peak", "precision"])
     ap.add_argument("--impl", default="lfg", choices=["lfg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--untuned", action="store_true",
@@ -346,6 +595,10 @@ def main():
     ap.add_argument("--batch", type=int, default=0,
                     help="override the batch of a c2c workload (smaller cases for profiling)")
     args = ap.parse_args()
+    if args.workload == "fp64_peak":
+        return run_fp64_peak(args)
+    if args.workload == "precision":
+        return run_precision(args)
     wl = dict(WORKLOADS[args.workload])
     if args.precision and wl["kind"] == "c2c" and wl.get("precision", "f64") != args.precision:
         wl["precision"] = args.precision
@@ -485,6 +738,9 @@ def main():
                              "same_bits": bool(torch.equal(y.view(torch.float64),
                                                            y2.view(torch.float64)))}
 
+    if wl["kind"] == "ragged" and rank == 0:
+        extra["accuracy"] = ragged_accuracy(sizes, host, y.cpu().numpy())
+
     # roofline of the dominant kernel (one launch per step for ragged and single-group sizes)
     esz = 8.0 if wl.get("precision") == "f32" else 16.0
     alg_bytes = 2 * esz * points         # read + write of the data once
@@ -511,9 +767,9 @@ def main():
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        gf, threads, sample = cpu_reference(wl, 5, 1, budget_s=20)
-        cpu = {"value": round(gf, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
-               "sample": sample}
+        cb = cpu_reference(wl, runs=10, budget_s=20)
+        cpu = {"value": round(cb["gflops"], 3), "unit": "GFLOP/s", "cores": cb["threads"],
+               "kind": "port", "sample": cb["sample"], "published": cb.get("published")}
 
     if rank == 0:
         config = workload_config(args.workload, wl)

@@ -29,7 +29,7 @@ typedef enum {
   LFG_ERR_INVALID = 2,     /* malformed arguments (null pointer, bad spec length ...)  */
   LFG_ERR_CUDA = 3,        /* a CUDA runtime call failed                              */
   LFG_ERR_NOMEM = 4,       /* host or device allocation failed                        */
-  LFG_ERR_TIMEOUT = 5      /* a bounded device-side wait gave up (ragged work queue)  */
+  LFG_ERR_TIMEOUT = 5      /* a bounded device-side wait gave up (binary32 tile copies) */
 } lfg_status;
 
 typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
@@ -41,6 +41,10 @@ typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
 #define LFG_NO_GRAPH 4u      /* ragged: launch directly instead of replaying a CUDA graph    */
 #define LFG_ADJOINT 8u       /* r2c/c2r: exact cotangent scaling of the adjoint (see below)  */
 #define LFG_NO_COMPENSATION 16u /* binary32: plain twiddle products in every pass             */
+/* Testing the recovery path only: the binary32 persistent kernel's tile waits give up at
+ * once (its bulk copies still land and are waited for before the kernel exits).  A call on
+ * such a plan computes nothing useful; lfg_device_status then returns LFG_ERR_TIMEOUT. */
+#define LFG_TEST_WAIT_GIVE_UP 32u
 
 typedef struct lfg_plan lfg_plan;
 

@@ -410,6 +410,7 @@ lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision prec
   p.in.dist = p.out.dist = (int64_t)n;
   p.empty = howmany == 0;
   p.no_comp = (flags & LFG_NO_COMPENSATION) != 0;
+  p.wait_give_up = (flags & LFG_TEST_WAIT_GIVE_UP) != 0;
   p.measure = (flags & LFG_MEASURE) != 0 && !radices;
   if (radices) {
     if (npass < 1 || npass > lfg::kMaxPass) return fail(LFG_ERR_INVALID, "bad pass count");

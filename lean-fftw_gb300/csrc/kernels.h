@@ -25,10 +25,12 @@ cudaError_t launch_group_f32(const GroupDesc& g, bool fwd, const void* in, void*
 
 // Persistent FP32 kernel with bulk-async (TMA) prefetch for back-to-back lines of one group
 // (input and output 16-byte aligned, C*M even); *status = 1 if a bounded wait gave up.
+// give_up (tests of the recovery path): every tile wait gives up at once.
 size_t stream_smem_bytes_f32(const GroupDesc& g);
 int stream_blocks_per_sm_f32(const GroupDesc& g);
 cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
-                              int64_t lines, unsigned grid, int* status, cudaStream_t stream);
+                              int64_t lines, unsigned grid, int* status, cudaStream_t stream,
+                              bool give_up = false);
 
 // Persistent FP32 kernel for tiles of strided sub-problems (three tile buffers: a stage
 // filled by asynchronous element copies, two work buffers); in and out 8-byte aligned.

@@ -90,6 +90,7 @@ struct Plan {
   unsigned ts_grid[2] = {0, 0};
   unsigned col_ts_grid = 0;     // binary32 column pass of a rank-2 real plan: persistent grid
   int* d_status = nullptr; // set to 1 on the device when a bounded wait gave up
+  bool wait_give_up = false;  // LFG_TEST_WAIT_GIVE_UP: tile waits give up at once (tests)
   // real transforms (kind R2C / C2R): rows of the last dimension, and for rank 2 the complex
   // transform along the first dimension (columns of the half spectrum)
   RealDesc real{};

@@ -739,7 +739,7 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     // into shared memory before it is written)
     if (p.stream && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)
       return launch_stream_f32(p.groups[0], p.fwd, ib, ob, p.howmany, p.stream_grid, p.d_status,
-                               stream);
+                               stream, p.wait_give_up);
     return launch(0, p.groups[0], ib, ob);
   }
   // two groups: the intermediate goes to `out` when it does not alias the input, else to the

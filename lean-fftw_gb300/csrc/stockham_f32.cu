@@ -64,9 +64,9 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Poll with an iteration limit; false if the phase did not complete in time.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
+// Poll at most `limit` times; false if the phase did not complete in time.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kSpinLimit) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_test(bar, parity)) return true;
   return false;
 }
@@ -77,11 +77,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 // current tile in two work buffers, so HBM reads overlap the arithmetic.  The first pass
 // reads the stage buffer directly, after which the buffer is refilled with a later tile.
 // A wait that gives up sets *status = 1, waits (bounded) for this CTA's copies in flight and
-// returns.
+// returns.  tile_limit bounds the tile waits (kSpinLimit; 0 in tests of the give-up path, whose
+// drain still uses kSpinLimit).
 template <bool FWD>
 __global__ void __launch_bounds__(kGroupThreads, 3)
 stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __restrict__ out,
-                  int64_t lines, int* status) {
+                  int64_t lines, int* status, uint32_t tile_limit) {
   extern __shared__ __align__(128) float2 smem_f32s[];
   __shared__ __align__(8) uint64_t bars[kStages];
   const int M = g.M, CM = g.C * g.M, PM = sub_pitch(g.M);
@@ -113,7 +114,7 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t l0 = tile * g.C;
     const int C = (int)min((int64_t)g.C, lines - l0);
-    const bool ok = __syncthreads_and(mbar_wait(&bars[s], (parity >> s) & 1));
+    const bool ok = __syncthreads_and(mbar_wait(&bars[s], (parity >> s) & 1, tile_limit));
     if (!ok) {
       failed = true;
       break;
@@ -308,13 +309,15 @@ int stream_blocks_per_sm_f32(const GroupDesc& g) {
 }
 
 cudaError_t launch_stream_f32(const GroupDesc& gd, bool fwd, const void* in, void* out,
-                              int64_t lines, unsigned grid, int* status, cudaStream_t stream) {
+                              int64_t lines, unsigned grid, int* status, cudaStream_t stream,
+                              bool give_up) {
   GroupDesc g = gd;
   set_divisors(g);
   if (lines <= 0) return cudaSuccess;
   auto kern = fwd ? stream_kernel_f32<true> : stream_kernel_f32<false>;
   kern<<<grid, kGroupThreads, stream_smem_bytes_f32(g), stream>>>(
-      g, static_cast<const float2*>(in), static_cast<float2*>(out), lines, status);
+      g, static_cast<const float2*>(in), static_cast<float2*>(out), lines, status,
+      give_up ? 0u : kSpinLimit);
   return cudaGetLastError();
 }
 

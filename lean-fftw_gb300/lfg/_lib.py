@@ -26,6 +26,8 @@ LFG_F32 = 1
 LFG_ESTIMATE = 0
 LFG_MEASURE = 1
 LFG_ADJOINT = 8
+LFG_NO_COMPENSATION = 16
+LFG_TEST_WAIT_GIVE_UP = 32
 
 
 class PlanInfo(ctypes.Structure):

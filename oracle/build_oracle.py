@@ -23,6 +23,7 @@ oracle.py.
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
 import os
 import platform
 import subprocess
@@ -39,6 +40,7 @@ ORACLE_RADICES = [2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 18, 20, 24
 
 # lean-fftw's own generated kernels cover these radices (LeanFFTW/Native/Kernels.lean)
 NATIVE_RADICES = (2, 4, 8, 16)
+GEN_PARTS = 6     # the generator's codelets are compiled as this many parallel sources
 
 
 def _write_if_changed(path: str, text: str) -> None:
@@ -51,22 +53,31 @@ def build(force: bool = False) -> str:
     sys.path.insert(0, HERE)
     import native_dag  # noqa: E402
     sys.path.insert(0, os.path.join(ROOT, "lean-fftw_gb300"))
-    from lfg.codegen.emit import c_codelets  # noqa: E402  (radices without published kernels)
+    # radices without published kernels: the restated generator's DAGs
+    from lfg.codegen.kernel import butterfly_k  # noqa: E402
+    from lfg.codegen.sexpr import cst_value  # noqa: E402
 
     os.makedirs(BUILD, exist_ok=True)
     so = os.path.join(BUILD, "liboracle.so")
     src = os.path.join(HERE, "refstock.c")
     trig = os.path.join(HERE, "trig_ref.c")
     nat = os.path.join(BUILD, "codelets_native.c")
-    cod = os.path.join(BUILD, "codelets_gen.c")
-    _write_if_changed(nat, native_dag.c_source(native_dag.load()))
-    # the generator's lookups are renamed: refstock.c asks the native kernels first
-    gen = c_codelets([R for R in ORACLE_RADICES if R not in NATIVE_RADICES])
-    gen = gen.replace("lfo_codelet_fn lfo_codelet(", "lfo_codelet_fn lfo_codelet_gen(")
-    gen = gen.replace("lfo_pass_fn lfo_pass(", "lfo_pass_fn lfo_pass_gen(")
-    _write_if_changed(cod, gen)
+    cods = [os.path.join(BUILD, f"codelets_gen{i}.c") for i in range(GEN_PARTS)]
+    _write_if_changed(nat, native_dag.c_source(native_dag.load(), "lfo_native"))
+    bits = lambda c: native_dag.bits_hex(cst_value(c))
+    gen = {}
+    for R in ORACLE_RADICES:
+        if R in NATIVE_RADICES:
+            continue
+        for fwd in (True, False):
+            for tw in (False, True):
+                k = butterfly_k(fwd, R, tw)
+                gen[native_dag.kernel_name(fwd, R, tw)] = native_dag.from_ops(
+                    R, fwd, tw, k.n_in, k.ops, k.outs, bits)
+    for path, text in zip(cods, native_dag.c_source(gen, "lfo_gen", parts=GEN_PARTS)):
+        _write_if_changed(path, text)
     if (not force and os.path.exists(so)
-            and os.path.getmtime(so) >= max(os.path.getmtime(p) for p in (src, cod, nat, trig))):
+            and os.path.getmtime(so) >= max(os.path.getmtime(p) for p in (src, nat, trig, *cods))):
         return so
     # -march/-mcpu=native: the host's vector units (x86 also gets hardware fma this way);
     # -ffp-contract=off still forbids fusing anything the kernels do not fuse
@@ -74,9 +85,17 @@ def build(force: bool = False) -> str:
         arch = ["-march=native", "-mfma"]
     else:
         arch = ["-mcpu=native"]
-    cmd = ["gcc", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
-           "-std=gnu11", *arch, "-o", so + ".tmp", src, trig, nat, cod, "-lm"]
-    subprocess.run(cmd, check=True)
+    flags = ["gcc", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+             "-std=gnu11", *arch]
+    srcs = (src, trig, nat, *cods)
+    objs = [os.path.join(BUILD, os.path.basename(c) + ".o") for c in srcs]
+    # the generated files are large: compile the sources in parallel
+    with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        for r in ex.map(lambda co: subprocess.run([*flags, "-c", co[0], "-o", co[1]]),
+                        zip(srcs, objs)):
+            if r.returncode != 0:
+                raise RuntimeError("oracle compile failed")
+    subprocess.run([*flags, "-shared", "-o", so + ".tmp", *objs, "-lm"], check=True)
     os.replace(so + ".tmp", so)
     return so
 

@@ -123,10 +123,12 @@ def counts(k: dict):
 
 # ------------------------------------------------------------------ C emission
 
-def _c_body(k: dict) -> List[str]:
+def _c_body(k: dict, x, y) -> List[str]:
+    """Statements of kernel k reading input slot i as the C expression x(i) and storing output
+    i with the C statement y(i, value)."""
     n_in = k["n_in"]
-    s = lambda i: f"x[{i}]" if i < n_in else f"t{i}"
-    lines = []
+    s = lambda i: f"in{i}" if i < n_in else f"t{i}"
+    lines = [f"const double in{i} = {x(i)};" for i in range(n_in)]
     for idx, op in enumerate(k["ops"]):
         o, slot = op[0], n_in + idx
         if o == "cst":
@@ -138,69 +140,112 @@ def _c_body(k: dict) -> List[str]:
             e = f"{s(op[1])} - {s(op[2])}"
         elif o == "mul":
             e = f"{s(op[1])} * {s(op[2])}"
+        elif o == "neg":
+            e = f"-{s(op[1])}"
         elif o == "fma":
             e = f"fma({s(op[1])}, {s(op[2])}, {s(op[3])})"
         elif o == "fms":
             e = f"fma({s(op[1])}, {s(op[2])}, -{s(op[3])})"
-        else:
+        elif o == "fnma":
             e = f"fma(-{s(op[1])}, {s(op[2])}, {s(op[3])})"
-        lines.append(f"  const double t{slot} = {e};")
-    lines += [f"  y[{i}] = {s(o)};" for i, o in enumerate(k["outs"])]
+        else:
+            raise ValueError(op)
+        lines.append(f"const double t{slot} = {e};")
+    lines += [y(i, s(o)) for i, o in enumerate(k["outs"])]
     return lines
 
 
-def c_source(kernels: Dict[str, dict]) -> str:
-    """C butterflies `lfo_native_bfly*` (compile with -ffp-contract=off) and one Stockham pass
-    per kernel with it inlined (the pass of Gen/Stockham.lean:263-284, as refstock.c's), plus
-    the lookups `lfo_native_codelet(fwd, R, tw)` and `lfo_native_pass(fwd, R, tw)`."""
-    out = ["/* ORACLE (test infrastructure only).  Generated by oracle/native_dag.py from",
-           " * tests/golden/native_kernels.json, the butterflies of lean-fftw's",
-           " * LeanFFTW/Native/Kernels.lean.  Compile with -ffp-contract=off. */",
-           "#include <math.h>", "#include <stddef.h>", "",
-           "typedef void (*lfo_codelet_fn)(const double *x, double *y);",
-           "typedef void (*lfo_pass_fn)(long N, long ns, const double *tw, const double *z,",
-           "                            double *o);", ""]
+def c_source(kernels: Dict[str, dict], prefix: str = "lfo_native", parts: int = 1):
+    """C butterflies `<prefix>_bfly*` (x: inputs in slot order, y: outputs) and one Stockham
+    pass per kernel with the butterfly inlined -- the pass of Gen/Stockham.lean:263-284:
+    butterfly j = b*ns + k reads z[j + r*N/R] and, twiddled, tw[m*ns + k] (m < 2(R-1)), and
+    writes output r at b*ns*R + k + r*ns -- plus the lookups `<prefix>_codelet(fwd, R, tw)`
+    and `<prefix>_pass(fwd, R, tw)`.  The passes loop over k innermost (unit-stride complex
+    accesses, so the compiler can vectorise across butterflies), or over b when ns = 1.
+    Compile with -ffp-contract=off: every operation is rounded as the kernel prescribes.
+    With parts > 1 the kernels are spread over `parts` sources (returned as a list, the
+    lookups in the last), so that they compile in parallel."""
+    head = ["/* ORACLE (test infrastructure only).  Generated by oracle/native_dag.py.",
+            " * Compile with -ffp-contract=off. */",
+            "#include <math.h>", "#include <stddef.h>", "",
+            "typedef void (*lfo_codelet_fn)(const double *x, double *y);",
+            "typedef void (*lfo_pass_fn)(long N, long ns, const double *tw, const double *z,",
+            "                            double *o);", ""]
+    files = [list(head) for _ in range(max(1, parts))]
+    load = [0] * len(files)
     table = []
-    for name in sorted(kernels, key=lambda n: (kernels[n]["R"], kernels[n]["tw"], not kernels[n]["fwd"])):
+    for name in sorted(kernels, key=lambda n: -len(kernels[n]["ops"])):
         k = kernels[name]
+        part = load.index(min(load))
+        load[part] += len(k["ops"])
+        out = files[part]
         R, tw = k["R"], k["tw"]
-        fn, pn = f"lfo_native_{name}", f"lfo_native_pass_{name}"
+        fn, pn = f"{prefix}_{name}", f"{prefix}_pass_{name}"
         out.append(f"void {fn}(const double *restrict x, double *restrict y) {{")
-        out += _c_body(k)
+        out += ["  " + l for l in _c_body(k, lambda i: f"x[{i}]", lambda i, v: f"y[{i}] = {v};")]
         out += ["}", ""]
-        out += [f"static void {pn}(long N, long ns, const double *restrict tw, "
+
+        def xin(i, zi, ti):
+            if i < 2 * R:
+                r, c = divmod(i, 2)
+                return f"{zi(r)}[{c}]"
+            return ti(i - 2 * R)
+
+        out += [f"void {pn}(long N, long ns, const double *restrict tw, "
                 "const double *restrict z, double *restrict o) {",
-                f"  const long NR = N / {R};",
-                "  for (long j = 0; j < NR; ++j) {",
-                "    const long kk = j % ns, b = j / ns;",
-                f"    double x[{k['n_in']}], y[{2 * R}];",
-                f"    for (int r = 0; r < {R}; ++r) {{",
-                "      x[2 * r] = z[2 * (j + r * NR)];",
-                "      x[2 * r + 1] = z[2 * (j + r * NR) + 1];",
-                "    }"]
-        if tw:
-            out += [f"    for (int r = 0; r < {2 * (R - 1)}; ++r) x[{2 * R} + r] = tw[r * ns + kk];"]
-        out += [f"    {fn}(x, y);",
-                f"    for (int r = 0; r < {R}; ++r) {{",
-                f"      const long c = b * ns * {R} + kk + r * ns;",
-                "      o[2 * c] = y[2 * r];",
-                "      o[2 * c + 1] = y[2 * r + 1];",
-                "    }",
-                "  }",
-                "}", ""]
+                f"  const long NR = N / {R}, NB = NR / ns;",
+                "  if (ns == 1) {",
+                "    for (long b = 0; b < NB; ++b) {"]
+        body1 = _c_body(k, lambda i: xin(i, lambda r: f"(z + 2 * (b + {r} * NR))",
+                                          lambda m: f"tw[{m}]"),
+                        lambda i, v: f"o[2 * (b * {R} + {i // 2}) + {i % 2}] = {v};")
+        out += ["      " + l for l in body1]
+        out += ["    }", "    return;", "  }",
+                "  for (long b = 0; b < NB; ++b) {",
+                "    const double *restrict zb = z + 2 * b * ns;",
+                f"    double *restrict ob = o + 2 * b * ns * {R};",
+                "    for (long kk = 0; kk < ns; ++kk) {"]
+        body = _c_body(k, lambda i: xin(i, lambda r: f"(zb + 2 * (kk + {r} * NR))",
+                                         lambda m: f"tw[{m} * ns + kk]"),
+                       lambda i, v: f"ob[2 * (kk + {i // 2} * ns) + {i % 2}] = {v};")
+        out += ["      " + l for l in body]
+        out += ["    }", "  }", "}", ""]
         table.append((int(k["fwd"]), R, int(tw), fn, pn))
+    out = files[-1]
+    for row in table:
+        out.append(f"void {row[3]}(const double *restrict x, double *restrict y);")
+        out.append(f"void {row[4]}(long N, long ns, const double *restrict tw, "
+                   "const double *restrict z, double *restrict o);")
+    table.sort(key=lambda r: (r[1], r[2], -r[0]))
     for what, col in (("codelet", 3), ("pass", 4)):
-        out.append(f"lfo_{what}_fn lfo_native_{what}(int fwd, int R, int tw) {{")
+        out.append(f"lfo_{what}_fn {prefix}_{what}(int fwd, int R, int tw) {{")
         for row in table:
             out.append(f"  if (fwd == {row[0]} && R == {row[1]} && tw == {row[2]}) return {row[col]};")
         out += ["  return NULL;", "}", ""]
-    return "\n".join(out)
+    texts = ["\n".join(f) for f in files]
+    return texts if parts > 1 else texts[0]
+
+
+def from_ops(R: int, fwd: bool, tw: bool, n_in: int, ops, outs, cst_bits) -> dict:
+    """A kernel in this module's encoding from an operation list in the same slot convention
+    (operations ("add"|"sub"|"mul", a, b), ("neg", a), ("fma"|"fms"|"fnma", a, b, c),
+    ("zero",), ("cst", c) with cst_bits(c) giving its 16-hex-digit binary64 bits)."""
+    conv = []
+    for op in ops:
+        if op[0] == "cst":
+            conv.append(["cst", cst_bits(op[1])])
+        elif op[0] == "zero":
+            conv.append(["cst", "0000000000000000"])
+        else:
+            conv.append([op[0], *op[1:]])
+    return {"R": R, "fwd": fwd, "tw": tw, "n_in": n_in, "ops": conv, "outs": list(outs)}
 
 
 # ------------------------------------------------------------------ exact evaluation
 
-def _bits(v: float) -> int:
-    return struct.unpack("<Q", struct.pack("<d", v))[0]
+def bits_hex(v: float) -> str:
+    """The 16 hex digits of a binary64 value's bits."""
+    return f"{struct.unpack('<Q', struct.pack('<d', v))[0]:016x}"
 
 
 def fma_exact(a: float, b: float, c: float) -> float:
@@ -245,6 +290,8 @@ def evaluate(k: dict, x: List[float]) -> List[float]:
             v.append(fma_exact(-v[op[2]], 1.0, v[op[1]]))
         elif o == "mul":
             v.append(fma_exact(v[op[1]], v[op[2]], -0.0))
+        elif o == "neg":
+            v.append(-v[op[1]])
         elif o == "fma":
             v.append(fma_exact(v[op[1]], v[op[2]], v[op[3]]))
         elif o == "fms":

@@ -30,27 +30,27 @@ typedef void (*lfo_codelet_fn)(const double *x, double *y);
 typedef void (*lfo_pass_fn)(long N, long ns, const double *tw, const double *z, double *o);
 lfo_codelet_fn lfo_native_codelet(int fwd, int R, int tw);
 lfo_pass_fn lfo_native_pass(int fwd, int R, int tw);
-lfo_codelet_fn lfo_codelet_gen(int fwd, int R, int tw);
-lfo_pass_fn lfo_pass_gen(int fwd, int R, int tw);
+lfo_codelet_fn lfo_gen_codelet(int fwd, int R, int tw);
+lfo_pass_fn lfo_gen_pass(int fwd, int R, int tw);
 
 /* The butterfly of radix R: lean-fftw's generated kernel where it ships one, else the
  * restated generator's. */
 lfo_codelet_fn lfo_codelet(int fwd, int R, int tw)
 {
      lfo_codelet_fn f = lfo_native_codelet(fwd, R, tw);
-     return f ? f : lfo_codelet_gen(fwd, R, tw);
+     return f ? f : lfo_gen_codelet(fwd, R, tw);
 }
 
 static lfo_pass_fn lfo_pass(int fwd, int R, int tw)
 {
      lfo_pass_fn f = lfo_native_pass(fwd, R, tw);
-     return f ? f : lfo_pass_gen(fwd, R, tw);
+     return f ? f : lfo_gen_pass(fwd, R, tw);
 }
 
 /* Evaluate one butterfly (x: 2R data values, then 2(R-1) twiddle values when tw; y: 2R). */
 int lfo_bfly(int fwd, int R, int tw, int native, const double *x, double *y)
 {
-     lfo_codelet_fn f = native ? lfo_native_codelet(fwd, R, tw) : lfo_codelet_gen(fwd, R, tw);
+     lfo_codelet_fn f = native ? lfo_native_codelet(fwd, R, tw) : lfo_gen_codelet(fwd, R, tw);
      if (!f) return -1;
      f(x, y);
      return 0;

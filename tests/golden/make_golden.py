@@ -14,6 +14,11 @@ Two kinds of fixture:
      xcheck.json           results/repro-2026-11-04/xcheck-bits.jsonl (chosen plan and
                            relative L2 error against long-double FFTW, 36 sizes)
      opcounts.json         docs/ITERATIONS.md:227-230 and :285-287 (kernel op counts)
+     accuracy_emr.json     results/emr-i12/accuracy.txt:1-36 (libbench2 --accuracy of the
+                           published engine, power-of-two sizes: forward and backward
+                           relative L1/L2/Linf errors against a multiple-precision FFT)
+     published_times.json  docs/RESULTS.md:72-89 (median single-core time of the published
+                           engine, i12, and of FFTW per power-of-two size, Emerald Rapids)
      native_kernels.json   LeanFFTW/Native/Kernels.lean:9-1897 (the sixteen generated
                            radix-2/4/8/16 butterflies, parsed by oracle/native_dag.py into
                            operation lists with their constant bits)
@@ -72,6 +77,33 @@ def copy_reference_pins(ref: str) -> None:
                    "twiddled8_total": int(m8.group(1)),
                    "source": "lean-fftw docs/ITERATIONS.md:61-62, 227-230, 285-287"}, f, indent=1)
     native_kernels(ref)
+    published_times(ref)
+    acc = {}
+    for line in open(os.path.join(ref, "results", "emr-i12", "accuracy.txt")):
+        d = json.loads(line)
+        if d["impl"] == "lean-i12" and d["rc"] == 0:
+            acc[str(d["n"])] = dict(zip(["fwd_l1", "fwd_l2", "fwd_linf", "bwd_l1", "bwd_l2",
+                                         "bwd_linf"], d["err"]))
+    with open(os.path.join(HERE, "accuracy_emr.json"), "w") as f:
+        json.dump({"source": "lean-fftw results/emr-i12/accuracy.txt (impl lean-i12, "
+                             "libbench2 --accuracy, problem ocfN)", "errors": acc}, f, indent=0)
+
+
+def published_times(ref: str) -> None:
+    unit = {"ns": 1e-9, "µs": 1e-6, "ms": 1e-3}
+    rows = {}
+    lines = open(os.path.join(ref, "docs", "RESULTS.md")).read().splitlines()
+    start = next(i for i, l in enumerate(lines) if l.startswith("| N | FFTW best | mode | i11 | i12"))
+    for i, line in enumerate(lines[start + 2:], start + 3):
+        m = re.match(r"\| (\d+) \| ([\d.]+) (ns|µs|ms) \| \w+ \| ([\d.]+) (ns|µs|ms) \| "
+                     r"([\d.]+) (ns|µs|ms) \|", line)
+        if not m:
+            break
+        rows[m.group(1)] = {"fftw_s": float(m.group(2)) * unit[m.group(3)],
+                            "i12_s": float(m.group(6)) * unit[m.group(7)], "line": i}
+    with open(os.path.join(HERE, "published_times.json"), "w") as f:
+        json.dump({"source": "lean-fftw docs/RESULTS.md (median of 10 runs, one core, "
+                             "libbench2 protocol)", "times": rows}, f, indent=0)
 
 
 def native_kernels(ref: str) -> None:

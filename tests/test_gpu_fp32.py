@@ -66,3 +66,33 @@ def test_compensation_helps_large_sizes(n):
     e_comp = O.rel_l2(_run(n, B, x, compensated=True), ref)
     e_plain = O.rel_l2(_run(n, B, x, compensated=False), ref)
     assert e_comp <= e_plain * 1.02, (e_comp, e_plain)
+
+
+def test_bounded_wait_recovery():
+    """The persistent binary32 kernel waits on its bulk copies with an iteration limit.  A
+    plan made with LFG_TEST_WAIT_GIVE_UP gives every tile wait up at once (the copies still
+    land, and each CTA waits for its own before it exits): the call reports LFG_ERR_TIMEOUT
+    through lfg_device_status, the status is then clear, and the next call of a normal plan
+    on the same data is correct to the bit."""
+    import ctypes
+    from lfg._lib import LFG_ERR_TIMEOUT, LFG_OK, LFG_TEST_WAIT_GIVE_UP, lib
+    n, B = 1024, 4096
+    x = torch.from_numpy(O.uniform_complex((B, n), seed=11).astype(np.complex64)).cuda()
+    h = ctypes.c_void_p()
+    assert lib().lfg_plan_1d(n, -1, B, 1, LFG_TEST_WAIT_GIVE_UP, ctypes.byref(h)) == LFG_OK
+    failing = lfg.Plan(h)
+    y = torch.zeros_like(x)
+    failing.execute(x, y)
+    assert lib().lfg_device_status(failing.handle) == LFG_ERR_TIMEOUT
+    assert lib().lfg_device_status(failing.handle) == LFG_OK        # cleared once read
+    good = lfg.plan_1d(n, -1, B, precision="f32")
+    ref = good.execute(x)
+    torch.cuda.synchronize()
+    assert lib().lfg_device_status(good.handle) == LFG_OK
+    again = torch.empty_like(x)
+    good.execute(x, again)
+    torch.cuda.synchronize()
+    assert torch.equal(again, ref)
+    ref64 = O.ref_transform(True, n, good.radices, x.cpu().numpy().astype(np.complex128)[:8])
+    e = O.rel_l2(ref[:8].cpu().numpy().astype(np.complex128), ref64)
+    assert e < 4 * U32 * np.sqrt(np.log2(n)), e
