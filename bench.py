@@ -8,7 +8,9 @@ Workloads (synthetic inputs, re/im iid uniform[-0.5, 0.5) from numpy default_rng
              log-uniformly from [2, 16384] and snapped to the nearest 13-smooth integer in
              log distance (859 distinct sizes, sum 14,922,904 points), packed back to back
              in size order; one persistent launch replayed from a CUDA graph.  The same batch
-             with one launch per distinct size is timed beside it (`per_size`).
+             with one launch per distinct size is timed beside it, the launches in one chain
+             (`per_size`) and spread over 16 independent graph branches so that different
+             sizes run at the same time (`per_size_concurrent`).
   c2c_<N>    1-D complex FP64 forward, N = 2^k (k = 1..18), batch 2^26 / N (1 GiB in and
              out): the power-of-two sweep.
   small_1024 one transform of N = 1024 (the plain small case: latency-bound).
@@ -636,6 +638,7 @@ def main():
         plan = lfg.plan_ragged(sizes, wl["sign"], measure=not args.untuned)   # autotuned
         t_plan = time.perf_counter() - t_plan
         per_size = lfg.plan_ragged(sizes, wl["sign"], per_size=True)
+        per_size_conc = lfg.plan_ragged(sizes, wl["sign"], per_size=True, concurrent=True)
         rinfo = plan.info()
         host = (rng.random((total, 2)) - 0.5).view(np.complex128).reshape(total)
         flops_step = float(sum(flops_per_transform(int(n)) for n in sizes))
@@ -724,19 +727,23 @@ def main():
     value = flops_step * ws / (ms * 1e-3) / 1e9
 
     if wl["kind"] == "ragged":
-        y2 = torch.empty_like(x)
-        ps_step = lambda: per_size.execute(x, y2)
-        for _ in range(3):
-            ps_step()
-        ps_ms, _ = timed(ps_step, min(20, max(5, args.steps // 4)), stream, local, barrier)
-        ps_ms = max_over_ranks(ps_ms, dev)
-        torch.cuda.synchronize()
-        extra["per_size"] = {"value": round(flops_step * ws / (ps_ms * 1e-3) / 1e9, 3),
-                             "unit": "GFLOP/s", "ms_per_step": round(ps_ms, 4),
-                             "launches_per_step": int(per_size.info().launches),
-                             "speedup_of_persistent": round(ps_ms / ms, 3),
-                             "same_bits": bool(torch.equal(y.view(torch.float64),
-                                                           y2.view(torch.float64)))}
+        # the comparison point: one launch per distinct size, in one chain (each size after
+        # the previous one) and spread over 16 independent graph branches (sizes overlap)
+        for key, ps_plan in (("per_size", per_size), ("per_size_concurrent", per_size_conc)):
+            y2 = torch.empty_like(x)
+            ps_step = lambda: ps_plan.execute(x, y2)
+            for _ in range(3):
+                ps_step()
+            ps_ms, _ = timed(ps_step, min(20, max(5, args.steps // 4)), stream, local, barrier)
+            ps_ms = max_over_ranks(ps_ms, dev)
+            torch.cuda.synchronize()
+            extra[key] = {"value": round(flops_step * ws / (ps_ms * 1e-3) / 1e9, 3),
+                          "unit": "GFLOP/s", "ms_per_step": round(ps_ms, 4),
+                          "launches_per_step": int(ps_plan.info().launches),
+                          "speedup_of_persistent": round(ps_ms / ms, 3),
+                          "same_bits": bool(torch.equal(y.view(torch.float64),
+                                                        y2.view(torch.float64)))}
+            del y2
 
     if wl["kind"] == "ragged" and rank == 0:
         extra["accuracy"] = ragged_accuracy(sizes, host, y.cpu().numpy())

@@ -38,6 +38,9 @@ typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
 #define LFG_ESTIMATE 0u      /* radix sequence with the fewest floating-point operations     */
 #define LFG_MEASURE 1u       /* time the leading candidates on the device, keep the fastest */
 #define LFG_PER_SIZE 2u      /* ragged: one launch per distinct size (the comparison point)  */
+#define LFG_PER_SIZE_CONCURRENT 64u /* ragged, with LFG_PER_SIZE: the per-size launches spread
+                                       over independent branches (streams / graph branches),
+                                       so different sizes run at the same time */
 #define LFG_NO_GRAPH 4u      /* ragged: launch directly instead of replaying a CUDA graph    */
 #define LFG_ADJOINT 8u       /* r2c/c2r: exact cotangent scaling of the adjoint (see below)  */
 #define LFG_NO_COMPENSATION 16u /* binary32: plain twiddle products in every pass             */

@@ -1137,6 +1137,7 @@ static lfg_status lfg_plan_ragged_impl(const int64_t* sizes, size_t count, const
   r.empty = count == 0;
   r.use_graph = !(flags & LFG_NO_GRAPH);
   r.per_size_mode = (flags & LFG_PER_SIZE) != 0;
+  r.per_size_concurrent = r.per_size_mode && (flags & LFG_PER_SIZE_CONCURRENT) != 0;
   r.sizes.assign(sizes, sizes + count);
   int64_t acc_in = 0, acc_out = 0;
   for (size_t i = 0; i < count; ++i) {

@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <numeric>
@@ -33,6 +34,10 @@ void free_ragged(RaggedPlan& r) {
   for (void* p : {r.d_twiddles, r.d_classes, r.d_items, r.d_in_off, r.d_out_off, r.d_counter,
                   r.d_host_in, r.d_host_out, r.d_slabs})
     if (p) cudaFree(p);
+  for (cudaStream_t st : r.branch_streams) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : r.branch_events) cudaEventDestroy(ev);
+  r.branch_streams.clear();
+  r.branch_events.clear();
   r.d_slabs = nullptr;
   r.graph_exec = nullptr;
   r.capture_stream = nullptr;
@@ -351,21 +356,70 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
       r.per_size.push_back(L);
     }
   }
+  if (r.per_size_mode && r.per_size_concurrent) {
+    // longest-processing-time assignment of the launches to the branches
+    std::vector<double> cost(r.per_size.size());
+    for (size_t i = 0; i < r.per_size.size(); ++i) {
+      const PerSizeLaunch& L = r.per_size[i];
+      const int64_t n = L.ngroups == 1 ? (int64_t)L.g[0].M : (int64_t)L.g[0].M * L.g[1].M;
+      const int64_t lines = L.ngroups == 1 ? L.g[0].total_sub : L.g[0].total_sub / std::max(1, L.g[0].nsub);
+      cost[i] = (double)n * (double)lines * std::log2((double)std::max<int64_t>(2, n));
+    }
+    std::vector<size_t> ord(cost.size());
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+    std::vector<double> load(kPerSizeBranches, 0.0);
+    r.per_size_branch.assign(r.per_size.size(), 0);
+    for (size_t i : ord) {
+      const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      r.per_size_branch[i] = b;
+      load[b] += cost[i];
+    }
+    for (int b = 0; b < kPerSizeBranches; ++b) {
+      cudaStream_t st = nullptr;
+      if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+        return "stream creation for the per-size branches failed";
+      r.branch_streams.push_back(st);
+    }
+    for (int b = 0; b <= kPerSizeBranches; ++b) {
+      cudaEvent_t ev = nullptr;
+      if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess)
+        return "event creation for the per-size branches failed";
+      r.branch_events.push_back(ev);
+    }
+  }
   return "";
 }
 
 cudaError_t execute_ragged_direct(const RaggedPlan& r, const void* in, void* out, cudaStream_t s) {
   if (r.per_size_mode) {
     const size_t es = r.precision == 0 ? 16 : 8;
-    for (const PerSizeLaunch& L : r.per_size) {
+    const bool conc = r.per_size_concurrent && !r.branch_streams.empty();
+    cudaError_t e = cudaSuccess;
+    if (conc) {
+      // fork: every branch starts after the work already queued on s
+      e = cudaEventRecord(r.branch_events[0], s);
+      for (size_t b = 0; b < r.branch_streams.size() && e == cudaSuccess; ++b)
+        e = cudaStreamWaitEvent(r.branch_streams[b], r.branch_events[0], 0);
+    }
+    for (size_t i = 0; i < r.per_size.size() && e == cudaSuccess; ++i) {
+      const PerSizeLaunch& L = r.per_size[i];
+      cudaStream_t st = conc ? r.branch_streams[r.per_size_branch[i]] : s;
       const char* ib = static_cast<const char*>(in) + L.in_base * es;
       char* ob = static_cast<char*>(out) + L.out_base * es;
-      for (int gi = 0; gi < L.ngroups; ++gi) {
-        cudaError_t e = launch_group_f64(L.g[gi], r.fwd, gi == 0 ? (const void*)ib : (const void*)ob, ob, s);
-        if (e != cudaSuccess) return e;
+      for (int gi = 0; gi < L.ngroups && e == cudaSuccess; ++gi)
+        e = launch_group_f64(L.g[gi], r.fwd, gi == 0 ? (const void*)ib : (const void*)ob, ob, st);
+    }
+    if (conc) {
+      // join: s continues after every branch (also on an error, so no branch is left open
+      // in a capture)
+      for (size_t b = 0; b < r.branch_streams.size(); ++b) {
+        cudaError_t e1 = cudaEventRecord(r.branch_events[1 + b], r.branch_streams[b]);
+        if (e1 == cudaSuccess) e1 = cudaStreamWaitEvent(s, r.branch_events[1 + b], 0);
+        if (e == cudaSuccess) e = e1;
       }
     }
-    return cudaSuccess;
+    return e;
   }
   cudaError_t e = cudaMemsetAsync(r.d_counter, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;

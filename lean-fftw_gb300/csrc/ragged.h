@@ -37,6 +37,12 @@ struct RaggedPlan {
   bool empty = false;
   bool use_graph = true;
   bool per_size_mode = false;
+  // per-size launches spread over kPerSizeBranches independent branches (cost-balanced; the
+  // launches of one size stay in order on one branch), joined at the end
+  bool per_size_concurrent = false;
+  std::vector<int> per_size_branch;                    // branch of each per-size launch
+  std::vector<cudaStream_t> branch_streams;
+  std::vector<cudaEvent_t> branch_events;              // [0]: fork, [1 + b]: join of branch b
   std::vector<int64_t> sizes, in_off, out_off;        // as given (complex elements)
   std::vector<int64_t> line_order;                     // lines sorted by size
   std::vector<int64_t> class_n, class_first, class_count;
@@ -59,6 +65,8 @@ struct RaggedPlan {
   mutable const void* graph_in = nullptr;
   mutable void* graph_out = nullptr;
 };
+
+constexpr int kPerSizeBranches = 16;
 
 std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt);
 cudaError_t execute_ragged(const RaggedPlan& r, const void* in, void* out, cudaStream_t s);

@@ -14,6 +14,7 @@ import numpy as np
 from ._lib import LFG_F64, LFG_MEASURE, check, lib
 
 LFG_PER_SIZE = 2
+LFG_PER_SIZE_CONCURRENT = 64
 LFG_NO_GRAPH = 4
 
 
@@ -105,6 +106,7 @@ class RaggedPlan:
 
 def plan_ragged(sizes: Sequence[int], sign: int = -1, in_offsets=None, out_offsets=None,
                 per_size: bool = False, graph: bool = True, measure: bool = False,
+                concurrent: bool = False,
                 tile_target: int = 0, single_max: int = 0, block_shape: int = 0,
                 radices: Optional[Dict[int, Sequence[int]]] = None) -> RaggedPlan:
     L = _bind()
@@ -112,7 +114,7 @@ def plan_ragged(sizes: Sequence[int], sign: int = -1, in_offsets=None, out_offse
     io = None if in_offsets is None else np.ascontiguousarray(in_offsets, dtype=np.int64)
     oo = None if out_offsets is None else np.ascontiguousarray(out_offsets, dtype=np.int64)
     flags = (LFG_PER_SIZE if per_size else 0) | (0 if graph else LFG_NO_GRAPH) | \
-            (LFG_MEASURE if measure else 0)
+            (LFG_MEASURE if measure else 0) | (LFG_PER_SIZE_CONCURRENT if concurrent else 0)
     tun = RaggedTuning(tile_target, single_max, 0, None, None, None, block_shape)
     keep = []
     if radices:

@@ -3,7 +3,7 @@
 Twiddles come from the binary64 exact-integer tables (rounded to binary32); sizes >= 2^16
 use compensated (hi, lo) twiddle products in their last passes.  The error is measured
 against the double-double DFT of the same (binary32) input and must stay at the binary32
-level (a few times 2^-24); compensation must not be worse than plain products.
+level (a few times 2^-24); compensated products must lower it at the largest sizes.
 """
 import numpy as np
 import pytest
@@ -60,12 +60,15 @@ def test_fp32_inplace_and_unaligned():
 
 @pytest.mark.parametrize("n", [1 << 16, 1 << 17, 1 << 18])
 def test_compensation_helps_large_sizes(n):
-    B = 2
+    """Compensated (hi, lo) twiddle products in the last passes remove the twiddles' own
+    binary32 rounding from those passes: the error must drop, by at least 1 % (measured:
+    2.2-2.5 % at 2^16-2^18; the rest of the binary32 error is the butterflies' rounding)."""
+    B = 4
     x = O.uniform_complex((B, n), seed=7).astype(np.complex64).astype(np.complex128)
     ref = O.dd_dft(True, x, nthreads=8)
     e_comp = O.rel_l2(_run(n, B, x, compensated=True), ref)
     e_plain = O.rel_l2(_run(n, B, x, compensated=False), ref)
-    assert e_comp <= e_plain * 1.02, (e_comp, e_plain)
+    assert e_comp < 0.99 * e_plain, (e_comp, e_plain)
 
 
 def test_bounded_wait_recovery():

@@ -36,7 +36,8 @@ def _check(plan, sizes, x, y_np, in_off, out_off):
     return bad
 
 
-@pytest.mark.parametrize("mode", ["graph", "direct", "per_size"])
+@pytest.mark.parametrize("mode", ["graph", "direct", "per_size", "per_size_concurrent",
+                                  "per_size_concurrent_direct"])
 def test_ragged_small_scattered(mode):
     rng = np.random.default_rng(3)
     sizes = np.array([2, 3, 16, 60, 60, 60, 1000, 4096, 2310, 7, 13, 13, 8192, 10368, 16384,
@@ -48,8 +49,8 @@ def test_ragged_small_scattered(mode):
     tin = int(in_off[-1] + sizes[-1] + 2)
     tout = int(out_off[-1] + sizes[-1] + 7)
     x = O.uniform_complex((tin,), seed=9)
-    plan = lfg.plan_ragged(sizes, -1, in_off, out_off, per_size=(mode == "per_size"),
-                           graph=(mode != "direct"))
+    plan = lfg.plan_ragged(sizes, -1, in_off, out_off, per_size=mode.startswith("per_size"),
+                           graph=not mode.endswith("direct"), concurrent="concurrent" in mode)
     xd = torch.from_numpy(x).cuda()
     yd = torch.full((tout,), SENT, dtype=torch.complex128, device="cuda")
     for _ in range(2):        # a second execution reuses the graph and the zeroed queue
@@ -76,12 +77,13 @@ def test_ragged_benchmark_batch_full():
     torch.cuda.synchronize()
     y = yd.cpu().numpy()
     assert not _check(plan, sizes, x, y, plan.in_offsets, plan.out_offsets)
-    # per-size strategy gives the same bits
-    ps = lfg.plan_ragged(sizes, -1, per_size=True)
-    y2 = torch.empty_like(xd)
-    ps.execute(xd, y2)
-    torch.cuda.synchronize()
-    assert torch.equal(y2.view(torch.float64), yd.view(torch.float64))
+    # per-size strategy gives the same bits, its launches in one chain or on 16 branches
+    for conc in (False, True):
+        ps = lfg.plan_ragged(sizes, -1, per_size=True, concurrent=conc)
+        y2 = torch.empty_like(xd)
+        ps.execute(xd, y2)
+        torch.cuda.synchronize()
+        assert torch.equal(y2.view(torch.float64), yd.view(torch.float64)), conc
 
 
 def test_ragged_host_entry():
