@@ -130,7 +130,10 @@ lfg_status lfg_execute(const lfg_plan *plan, const void *in, void *out, void *st
  * 16 MiB for two-group plans (LFG_ERR_UNSUPPORTED otherwise).  The array's device address is
  * looked up on the first call on each device, so make that first call before any stream
  * capture.  All calls share the one array: calls whose executions overlap on the GPU race on
- * it.  `data` is the device buffer given to the plan as both input and output. */
+ * it.  `data` is the device buffer given to the plan as both input and output.  Only plans
+ * that run as one or two Stockham pass groups are taken (1-D, 13-smooth, one batch
+ * dimension); plans of other algorithms (prime factors above 13, split or strided layouts)
+ * keep buffers of their own and are refused with LFG_ERR_UNSUPPORTED before anything runs. */
 lfg_status lfg_execute_inplace_static(const lfg_plan *plan, void *data, void *stream);
 
 /* Execute on host pointers: copies the spanned input to the device, transforms, copies the
@@ -246,6 +249,27 @@ const char *lfg_last_error(void);
 /* cos/sin(2*pi*m/n) for m < n as binary64, interleaved, from exact integer arithmetic:
  * lean-fftw's `Trig.cosSin2PiTable` (LeanFFTW/Core/Trig.lean:131-134). out: 2n doubles. */
 lfg_status lfg_cos_sin_table(uint64_t n, double *out);
+
+/* ---- lean-fftw's fast-engine entry points, for the libbench2 backend ------------------
+ * The same arguments as lean-fftw's `lfa_plan_measure` and `lfa_call`, in plain C.
+ *
+ * lfg_lfa_plan_measure replaces `lfa_plan_measure(N, fwd, in, out)`
+ * (LeanFFTW/Asm/Planner.lean:293-302): plans a binary64 1-D complex transform of size N
+ * (forward when fwd != 0) for the caller's host arrays at addresses in and out (in == out:
+ * in place), measuring candidate schedules on the device (LFG_MEASURE).  As with the
+ * reference, the arrays' contents may be overwritten (this implementation leaves them as they
+ * are).  Returns an opaque record, or NULL where the reference returns its empty plan: N
+ * outside 2..2^24 or with a prime factor above 13 (message in lfg_last_error()).
+ *
+ * lfg_lfa_call has the signature and meaning of `lfa_call(record, in, out)`
+ * (LeanFFTW/Asm/Kernels.lean:1203-1204, bench/backends/bench-leanfftw.c:284-288): the transform
+ * of the host array in (2N doubles, interleaved) written to out, returning when out holds it.
+ * It returns nothing, as lfa_call; lfg_lfa_status(record) gives the status of the record's last
+ * call.  lfg_lfa_release frees the record (the reference's lean_dec of its plan array). */
+const void *lfg_lfa_plan_measure(size_t N, uint8_t fwd, size_t in, size_t out);
+void lfg_lfa_call(const void *record, const double *in, double *out);
+lfg_status lfg_lfa_status(const void *record);
+void lfg_lfa_release(const void *record);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,19 @@ def _declared():
     return sorted(set(re.findall(r"\b(lfg_[a-z0-9_]+)\s*\(", text)))
 
 
+def test_libbench2_backend_builds_and_links():
+    """The libbench2 backend compiles against the stand-in libbench2 header, links against
+    liblfg.so and exports libbench2's backend interface (its GPU test drives it)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "libbench2_stub"))
+    import build_harness
+    lfg.lib()
+    L = ctypes.CDLL(build_harness.build())
+    for name in ("can_do", "setup", "doit", "done", "main_init", "initial_cleanup",
+                 "final_cleanup", "bench_doc", "lfgb_run"):
+        assert hasattr(L, name), name
+
+
 def test_exports_every_declared_symbol():
     L = lfg.lib()
     names = _declared()
