@@ -43,27 +43,32 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 template <class Lines>
 __device__ __forceinline__ void stage_tile(double2* X, const GroupDesc& g, const Lines& lines,
                                            int64_t s0, int C, const double2* src) {
+  // descriptor fields in registers: each cp.async below is a compiler memory barrier, after
+  // which fields read through a reference would be loaded again for every element
   const int64_t sub_st = g.in_sub, elem_st = g.in_elem;
   const int M = g.M;
   const int nsub = g.nsub;
+  const int gC = g.C;
+  const FastDiv fd_m = g.fd_m, fd_c = g.fd_c, fd_nsub = g.fd_nsub;
+  const Lines L = lines;
   const bool elem_fast = elem_st == 1;
   const int64_t line0 = s0 / nsub;
   const int sub0 = (int)(s0 - line0 * nsub);
-  const int nn = elem_fast ? C * M : g.C * M;
+  const int nn = elem_fast ? C * M : gC * M;
   const int PM = sub_pitch(M);
   for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
     int c, i;
     if (elem_fast) {
-      c = fdiv(idx, g.fd_m);
+      c = fdiv(idx, fd_m);
       i = idx - c * M;
     } else {
-      i = fdiv(idx, g.fd_c);
-      c = idx - i * g.C;
+      i = fdiv(idx, fd_c);
+      c = idx - i * gC;
       if (c >= C) continue;
     }
     const int t = sub0 + c;
-    const int ql = fdiv(t, g.fd_nsub);
-    const int64_t a = lines.in(line0 + ql) + (int64_t)(t - ql * nsub) * sub_st + (int64_t)i * elem_st;
+    const int ql = fdiv(t, fd_nsub);
+    const int64_t a = L.in(line0 + ql) + (int64_t)(t - ql * nsub) * sub_st + (int64_t)i * elem_st;
     cp_async16(X + c * PM + spad(i), src + a);
   }
   cp_async_commit();

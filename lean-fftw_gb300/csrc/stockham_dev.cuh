@@ -98,7 +98,7 @@ template <class T, bool FWD, int R, int MODE, bool SRCPAD, class Out>
 __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ src,
                                        const Out& out, int C, int M,
                                        const PassDesc& pd, int sub0, int nsub,
-                                       const FastDiv& fd_nsub) {
+                                       const FastDiv fd_nsub) {
   using P = Prec<T>;
   using Cx = typename P::C;
   constexpr bool TW = MODE == 1;
@@ -168,7 +168,7 @@ __device__ __forceinline__ void pass_t(const typename Prec<T>::C* __restrict__ s
 template <class T, bool FWD, bool SRCPAD = true, class Out>
 __device__ __forceinline__ void run_pass_to(const typename Prec<T>::C* src, const Out& out,
                                             int C, int M, const PassDesc& pd, int sub0, int nsub,
-                                            const FastDiv& fd_nsub) {
+                                            const FastDiv fd_nsub) {
 #define LFG_PASS_CASE(RR)                                                                        \
   case RR:                                                                                       \
     if (!pd.tw) pass_t<T, FWD, RR, 0, SRCPAD>(src, out, C, M, pd, sub0, nsub, fd_nsub);          \
@@ -201,7 +201,7 @@ __device__ __forceinline__ void run_pass_to(const typename Prec<T>::C* src, cons
 template <class T, bool FWD, bool SRCPAD = true>
 __device__ __forceinline__ void run_pass_t(const typename Prec<T>::C* src, typename Prec<T>::C* dst,
                                            int C, int M, const PassDesc& pd, int sub0, int nsub,
-                                           const FastDiv& fd_nsub) {
+                                           const FastDiv fd_nsub) {
   run_pass_to<T, FWD, SRCPAD>(src, SmemOut<T>{dst, sub_pitch(M)}, C, M, pd, sub0, nsub, fd_nsub);
 }
 
@@ -232,18 +232,23 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
                                           typename Prec<T>::C* gout, const GroupDesc& g,
                                           const Lines& lines, int64_t s0, int C) {
   using P = Prec<T>;
+  // descriptor fields in registers: the loops below store through generic pointers, after
+  // which fields read through a reference would be loaded again every iteration
   const int64_t sub_st = LOAD ? g.in_sub : g.out_sub;
   const int64_t elem_st = LOAD ? g.in_elem : g.out_elem;
   const int M = g.M;
   const int nsub = g.nsub;
+  const int gC = g.C;
+  const FastDiv fd_m = g.fd_m, fd_c = g.fd_c, fd_nsub = g.fd_nsub;
+  const Lines L = lines;
   const int n = C * M;
   const bool elem_fast = (elem_st == 1);
-  if (elem_fast && nsub == 1 && lines.pitch(LOAD) == M && g.unit_scale) {
+  if (elem_fast && nsub == 1 && L.pitch(LOAD) == M && g.unit_scale) {
     // back-to-back lines: the tile is one contiguous range of global memory
-    const int64_t base = (LOAD ? lines.in(s0) : lines.out(s0));
+    const int64_t base = (LOAD ? L.in(s0) : L.out(s0));
     const int PM = sub_pitch(M);
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
-      const int c = fdiv(idx, g.fd_m);
+      const int c = fdiv(idx, fd_m);
       const int t = c * PM + spad(idx - c * M);
       if (LOAD) tile[t] = gin[base + idx];
       else gout[base + idx] = tile[t];
@@ -255,25 +260,25 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
   const int sub0 = (int)(s0 - line0 * nsub);
   // strided sub-problems: neighbouring threads take neighbouring sub-problems, over the full
   // tile width g.C (a partial last tile skips the missing columns)
-  const int nn = elem_fast ? n : g.C * M;
+  const int nn = elem_fast ? n : gC * M;
   const bool unit = g.unit_scale != 0;
   const T sc = sizeof(T) == 4 ? (T)g.scale_f32 : (T)g.scale;
   const int PM = sub_pitch(M);
   for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
     int c, i;
     if (elem_fast) {
-      c = fdiv(idx, g.fd_m);
+      c = fdiv(idx, fd_m);
       i = idx - c * M;
     } else {
-      i = fdiv(idx, g.fd_c);
-      c = idx - i * g.C;
+      i = fdiv(idx, fd_c);
+      c = idx - i * gC;
       if (c >= C) continue;
     }
     const int t = sub0 + c;
-    const int ql = fdiv(t, g.fd_nsub);
+    const int ql = fdiv(t, fd_nsub);
     const int64_t line = line0 + ql;
     const int64_t sub = t - ql * nsub;
-    const int64_t a = (LOAD ? lines.in(line) : lines.out(line)) + sub * sub_st + (int64_t)i * elem_st;
+    const int64_t a = (LOAD ? L.in(line) : L.out(line)) + sub * sub_st + (int64_t)i * elem_st;
     if (LOAD) {
       tile[c * PM + spad(i)] = gin[a];
     } else if (unit) {
@@ -312,14 +317,19 @@ __device__ __forceinline__ typename Prec<T>::C* run_passes(const GroupDesc& g,
 template <class T, class Lines>
 struct GlobalRows {
   typename Prec<T>::C* dst;
-  const GroupDesc& g;
+  FastDiv fd_nsub;       // the group's fields it needs, held by value (registers)
+  int nsub;
+  int64_t out_sub;
   Lines lines;
   int64_t line0;
   int sub0;
+  __device__ __forceinline__ GlobalRows(typename Prec<T>::C* d, const GroupDesc& g, Lines l,
+                                        int64_t l0, int s0)
+      : dst(d), fd_nsub(g.fd_nsub), nsub(g.nsub), out_sub(g.out_sub), lines(l), line0(l0), sub0(s0) {}
   __device__ __forceinline__ typename Prec<T>::C* row(int c) const {
     const int t = sub0 + c;
-    const int ql = fdiv(t, g.fd_nsub);
-    return dst + lines.out(line0 + ql) + (int64_t)(t - ql * g.nsub) * g.out_sub;
+    const int ql = fdiv(t, fd_nsub);
+    return dst + lines.out(line0 + ql) + (int64_t)(t - ql * nsub) * out_sub;
   }
   __device__ __forceinline__ void put(typename Prec<T>::C* row, int i, typename Prec<T>::C v) const {
     row[i] = v;

@@ -183,26 +183,29 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // element order and addressing as the synchronous tile load (stockham_dev.cuh: copy_tile).
 __device__ __forceinline__ void load_tile_async(float2* S, const float2* in, const GroupDesc& g,
                                                 int64_t s0, int C) {
-  const int M = g.M, nsub = g.nsub, PM = sub_pitch(M);
+  // descriptor fields in registers (each cp.async is a compiler memory barrier)
+  const int M = g.M, nsub = g.nsub, PM = sub_pitch(M), gC = g.C;
+  const int64_t in_line = g.in_line, in_sub = g.in_sub, in_elem = g.in_elem;
+  const FastDiv fd_m = g.fd_m, fd_c = g.fd_c, fd_nsub = g.fd_nsub;
   const int64_t line0 = s0 / nsub;
   const int sub0 = (int)(s0 - line0 * nsub);
-  const bool elem_fast = g.in_elem == 1;
-  const int nn = elem_fast ? C * M : g.C * M;
+  const bool elem_fast = in_elem == 1;
+  const int nn = elem_fast ? C * M : gC * M;
 #pragma unroll 4
   for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
     int c, i;
     if (elem_fast) {
-      c = fdiv(idx, g.fd_m);
+      c = fdiv(idx, fd_m);
       i = idx - c * M;
     } else {
-      i = fdiv(idx, g.fd_c);
-      c = idx - i * g.C;
+      i = fdiv(idx, fd_c);
+      c = idx - i * gC;
       if (c >= C) continue;
     }
     const int t = sub0 + c;
-    const int ql = fdiv(t, g.fd_nsub);
-    const int64_t a = (line0 + ql) * g.in_line + (int64_t)(t - ql * nsub) * g.in_sub +
-                      (int64_t)i * g.in_elem;
+    const int ql = fdiv(t, fd_nsub);
+    const int64_t a = (line0 + ql) * in_line + (int64_t)(t - ql * nsub) * in_sub +
+                      (int64_t)i * in_elem;
     cp_async8(S + c * PM + spad(i), in + a);
   }
   cp_async_commit();

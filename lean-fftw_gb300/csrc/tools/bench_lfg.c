@@ -6,9 +6,10 @@
  *    at setup, lfg_lfa_call in the timed loop (the reference's lfa_plan_measure / lfa_call,
  *    bench-leanfftw.c:225-297);
  *  - every other problem goes through lean-fftw's FFI problem encoding
- *    (LeanFFTW/FFI.lean:13-47): the spanned input and output ranges of doubles, with the
- *    real and imaginary bases as offsets into them, planned by lfg_plan_spec and run on the
- *    host ranges by lfg_execute_host.
+ *    (LeanFFTW/FFI.lean:13-47): each side's spanned range of doubles (two ranges for split
+ *    complex data) is staged back to back in a private host buffer, the real and imaginary
+ *    bases become offsets into it, lfg_plan_spec plans the problem and lfg_execute_host runs
+ *    it on the staging buffers; the output ranges are copied back.
  *
  * Built against libbench2's bench-user.h this links into libbench2's benchmark program;
  * the tests build it against a stand-in header (tests/libbench2_stub) and drive
@@ -31,7 +32,6 @@ END_BENCH_DOC
 
 static const void *fast_rec = 0;   /* fast-engine record (lfg_lfa_plan_measure) */
 static lfg_plan *spec_plan = 0;    /* everything else (lfg_plan_spec) */
-static double *in_base, *out_base; /* low ends of the spanned input and output ranges */
 
 /* One side of a problem: bases of the real and imaginary parts, and the number of doubles
  * per unit of the problem's strides (2 for interleaved complex data, 1 otherwise). */
@@ -95,8 +95,7 @@ static void make_sides(const bench_problem *p, side_t *si, side_t *so)
      }
 }
 
-/* Offsets (in units of the problem's strides) of the lowest and highest element of one side
- * (the highest is not needed: lfg_plan_spec computes each side's span itself). */
+/* Offsets (in units of the problem's strides) of the lowest and highest element of one side. */
 static void stride_span(const bench_problem *p, int output, int half_last, long *lo, long *hi)
 {
      int d;
@@ -113,35 +112,63 @@ static void stride_span(const bench_problem *p, int output, int half_last, long 
      }
 }
 
-/* The low end of a side's spanned range of doubles and its re / im offsets from it. */
-static double *side_range(const side_t *s, long lo, double *off_re, double *off_im)
+/* Where a side's data lives: one range of doubles (real data, or interleaved complex data,
+ * whose imaginary parts sit inside it), or two ranges of equal length (split complex data;
+ * the real and imaginary arrays may be separate allocations).  The library runs on a private
+ * staging buffer holding the range(s) back to back, so nothing outside the caller's own
+ * elements is ever read or written. */
+typedef struct {
+     double *part[2];   /* start of each range in the caller's memory */
+     size_t len;        /* doubles per range */
+     int nparts;
+     double off_re, off_im;   /* FFI offsets of the re / im bases in the staging buffer */
+     double *stage;
+} staged_t;
+
+static void stage_layout(const side_t *s, long lo, long hi, staged_t *st)
 {
-     double *a = s->re + lo * s->mul;
-     if (!s->real && s->im + lo * s->mul < a) a = s->im + lo * s->mul;
-     *off_re = (double) (s->re - a);
-     *off_im = (double) (s->im - a);
-     return a;
+     st->len = (size_t) ((hi - lo) * s->mul + (s->real || s->mul == 1 ? 1 : 2));
+     st->part[0] = s->re + lo * s->mul;
+     st->nparts = (!s->real && s->mul == 1) ? 2 : 1;
+     st->part[1] = st->nparts == 2 ? s->im + lo * s->mul : 0;
+     st->off_re = (double) (-lo * s->mul);
+     st->off_im = st->nparts == 2 ? (double) st->len - (double) (lo * s->mul)
+                                  : st->off_re + (s->real ? 0 : 1);
+     st->stage = 0;
 }
 
-/* lean-fftw's FFI encoding of the problem (LeanFFTW/FFI.lean:13-21), relative to the low ends
- * of the spanned ranges; returns the number of doubles written, or 0 for rank 0. */
-static int encode(const bench_problem *p, double *spec, double **lo_in, double **lo_out)
+static void stage_copy(staged_t *st, int to_stage)
+{
+     int k;
+     for (k = 0; k < st->nparts; ++k) {
+          if (to_stage) memcpy(st->stage + k * st->len, st->part[k], st->len * sizeof(double));
+          else memcpy(st->part[k], st->stage + k * st->len, st->len * sizeof(double));
+     }
+}
+
+static staged_t stin, stout;
+
+/* lean-fftw's FFI encoding of the problem (LeanFFTW/FFI.lean:13-21), with the offsets of the
+ * staging layouts; returns the number of doubles written. */
+static int encode(const bench_problem *p, double *spec, staged_t *si_st, staged_t *so_st)
 {
      side_t si, so;
      long ilo, ihi, olo, ohi;
-     double offs[4];
      int k = 0, d;
      const int r = p->sz->rnk, v = p->vecsz->rnk;
      make_sides(p, &si, &so);
      stride_span(p, 0, p->kind == PROBLEM_REAL && p->sign > 0, &ilo, &ihi);
      stride_span(p, 1, p->kind == PROBLEM_REAL && p->sign < 0, &olo, &ohi);
-     *lo_in = side_range(&si, ilo, &offs[0], &offs[1]);
-     *lo_out = side_range(&so, olo, &offs[2], &offs[3]);
+     stage_layout(&si, ilo, ihi, si_st);
+     stage_layout(&so, olo, ohi, so_st);
      spec[k++] = p->kind == PROBLEM_COMPLEX ? 0 : p->kind == PROBLEM_REAL ? 1 : 2;
      spec[k++] = p->sign;
      spec[k++] = r;
      spec[k++] = v;
-     for (d = 0; d < 4; ++d) spec[k++] = offs[d];
+     spec[k++] = si_st->off_re;
+     spec[k++] = si_st->off_im;
+     spec[k++] = so_st->off_re;
+     spec[k++] = so_st->off_im;
      for (d = 0; d < r + v; ++d) {
           const bench_iodim *io = d < r ? &p->sz->dims[d] : &p->vecsz->dims[d - r];
           spec[k++] = io->n;
@@ -152,24 +179,24 @@ static int encode(const bench_problem *p, double *spec, double **lo_in, double *
      return k;
 }
 
-static lfg_plan *plan_problem(const bench_problem *p, double **lo_in, double **lo_out)
+static lfg_plan *plan_problem(const bench_problem *p, staged_t *si_st, staged_t *so_st)
 {
      double spec[8 + 4 * 64];
      lfg_plan *plan = 0;
      int nspec;
      if (p->sz->rnk + p->vecsz->rnk > 64) return 0;
-     nspec = encode(p, spec, lo_in, lo_out);
+     nspec = encode(p, spec, si_st, so_st);
      if (lfg_plan_spec(spec, (size_t) nspec, LFG_F64, LFG_ESTIMATE, &plan) != LFG_OK) return 0;
      return plan;
 }
 
 int can_do(bench_problem *p)
 {
-     double *a, *b;
+     staged_t a, b;
      lfg_plan *plan;
      if (!BENCH_FINITE_RNK(p->sz->rnk) || !BENCH_FINITE_RNK(p->vecsz->rnk)) return 0;
      if (fast_engine_problem(p)) return 1;
-     plan = plan_problem(p, &a, &b);    /* what lfg_plan_spec accepts */
+     plan = plan_problem(p, &a, &b);    /* what lfg_plan_spec accepts (nothing is touched) */
      if (!plan) return 0;
      lfg_destroy(plan);
      return 1;
@@ -182,8 +209,12 @@ void setup(bench_problem *p)
                                           (size_t) p->in, (size_t) p->out);
           if (fast_rec) return;
      }
-     spec_plan = plan_problem(p, &in_base, &out_base);
-     if (!spec_plan) {
+     spec_plan = plan_problem(p, &stin, &stout);
+     if (spec_plan) {
+          stin.stage = (double *) malloc(stin.nparts * stin.len * sizeof(double));
+          stout.stage = (double *) malloc(stout.nparts * stout.len * sizeof(double));
+     }
+     if (!spec_plan || !stin.stage || !stout.stage) {
           fprintf(stderr, "lean-fftw-gb300: problem not supported: %s\n", lfg_last_error());
           bench_exit(1);
      }
@@ -202,11 +233,18 @@ void doit(int iter, bench_problem *p)
           }
           return;
      }
-     for (it = 0; it < iter; ++it)
-          if (lfg_execute_host(spec_plan, in_base, out_base) != LFG_OK) {
+     for (it = 0; it < iter; ++it) {
+          /* the output ranges come along too: elements between a strided output's own keep
+           * the caller's values */
+          stage_copy(&stin, 1);
+          stage_copy(&stout, 1);
+          if (lfg_execute_host(spec_plan, stin.stage, stout.stage) != LFG_OK) {
                fprintf(stderr, "lean-fftw-gb300: %s\n", lfg_last_error());
                bench_exit(1);
+               return;
           }
+          stage_copy(&stout, 0);
+     }
 }
 
 void done(bench_problem *p)
@@ -214,6 +252,9 @@ void done(bench_problem *p)
      (void) p;
      if (fast_rec) lfg_lfa_release(fast_rec);
      if (spec_plan) lfg_destroy(spec_plan);
+     free(stin.stage);
+     free(stout.stage);
+     stin.stage = stout.stage = 0;
      fast_rec = 0;
      spec_plan = 0;
 }
