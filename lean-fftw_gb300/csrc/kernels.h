@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdint>
+#include <vector>
 
 #include "stockham.h"
 
@@ -25,12 +27,17 @@ cudaError_t launch_group_f32(const GroupDesc& g, bool fwd, const void* in, void*
 
 // Persistent FP32 kernel with bulk-async (TMA) prefetch for back-to-back lines of one group
 // (input and output 16-byte aligned, C*M even); *status = 1 if a bounded wait gave up.
-// give_up (tests of the recovery path): every tile wait gives up at once.
+// give_up (tests of the recovery path): every tile wait gives up at once.  variant: -1 for
+// any plan, or stream_variant_f32's index of a power-of-two plan compiled with its passes as
+// constants (the same bits, less index arithmetic).
 size_t stream_smem_bytes_f32(const GroupDesc& g);
-int stream_blocks_per_sm_f32(const GroupDesc& g);
+int stream_blocks_per_sm_f32(const GroupDesc& g, int variant = -1);
 cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                               int64_t lines, unsigned grid, int* status, cudaStream_t stream,
-                              bool give_up = false);
+                              bool give_up = false, int variant = -1);
+// Index of the compile-time variant of the persistent binary32 kernel for a one-group plan of
+// size n with radices rs, or -1.
+int stream_variant_f32(int64_t n, const std::vector<int>& rs);
 
 // Persistent FP32 kernel for tiles of strided sub-problems (three tile buffers: a stage
 // filled by asynchronous element copies, two work buffers); in and out 8-byte aligned.

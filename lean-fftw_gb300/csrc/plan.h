@@ -84,6 +84,7 @@ struct Plan {
   // binary32 single-group plans over back-to-back lines run the persistent bulk-copy kernel
   bool stream = false;
   unsigned stream_grid = 0;
+  int stream_variant = -1;      // compile-time power-of-two variant of that kernel (-1: none)
   // binary32 groups not covered by the stream kernel: the persistent strided-tile kernel
   // (asynchronous copies of the next tile), one grid per group
   bool tile_stream = false;

@@ -454,7 +454,10 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       const int64_t tiles = (p.howmany + g0.C - 1) / g0.C;
-      const int64_t want = (int64_t)sms * stream_blocks_per_sm_f32(g0);
+      bool any_comp = false;
+      for (int t = 0; t < g0.npass; ++t) any_comp = any_comp || g0.pass[t].comp;
+      p.stream_variant = any_comp ? -1 : stream_variant_f32(N, rs);
+      const int64_t want = (int64_t)sms * stream_blocks_per_sm_f32(g0, p.stream_variant);
       p.stream_grid = (unsigned)std::max<int64_t>(1, std::min(want, tiles));
       p.stream = true;
     }
@@ -739,7 +742,7 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     // into shared memory before it is written)
     if (p.stream && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)
       return launch_stream_f32(p.groups[0], p.fwd, ib, ob, p.howmany, p.stream_grid, p.d_status,
-                               stream, p.wait_give_up);
+                               stream, p.wait_give_up, p.stream_variant);
     return launch(0, p.groups[0], ib, ob);
   }
   // two groups: the intermediate goes to `out` when it does not alias the input, else to the

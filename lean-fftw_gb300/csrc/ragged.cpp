@@ -48,9 +48,18 @@ void free_ragged(RaggedPlan& r) {
 
 namespace {
 
-// Operations of a tile of C sub-problems of length M through passes t0..t1 of rs, and the
-// lane-slots they occupy: a pass of nb = C * M / R butterflies issues ceil(nb / 32) warps,
-// so a partial last warp leaves lanes of the FP64 pipe idle.
+// Butterflies per unit of pass time: a CTA's warp w runs on SM sub-partition w % 4, whose
+// FP64 pipe takes a whole warp instruction whatever its active lanes, so a pass of nb
+// butterflies keeps the busiest sub-partition for ceil(nb / 128) units of 128 butterflies
+// (ceil(nb / 32) warps spread round-robin over 4 sub-partitions).
+constexpr int64_t kPassGrain = 4 * 32;
+// Fixed cost of one tile (staging the next tile, the store phase, barriers, queue), in
+// binary64 operations of pass work: about 9000 per tile of the 8192-size batch on GB300
+// (clock64 stamps around each phase of the kernel).
+constexpr double kTileOverheadOps = 9000.0;
+
+// Pass time of a tile of C sub-problems of length M through passes t0..t1 of rs, in
+// operation-slots (SMSP-granular, see kPassGrain), and the operations it performs.
 void tile_lane_cost(int64_t C, int64_t M, const std::vector<int>& rs, int t0, int t1,
                     double* ops, double* slots) {
   for (int t = t0; t < t1; ++t) {
@@ -58,26 +67,28 @@ void tile_lane_cost(int64_t C, int64_t M, const std::vector<int>& rs, int t0, in
     const int64_t nb = C * (M / R);
     const double o = t == 0 ? kOpsUntw[R] : kOpsTw[R];
     *ops += (double)nb * o;
-    *slots += (double)(32 * ((nb + 31) / 32)) * o;
+    *slots += (double)(kPassGrain * ((nb + kPassGrain - 1) / kPassGrain)) * o;
   }
 }
 
 // Tile width for `total` sub-problems in tiles of at most cmax: the C in [cmax/2, cmax] whose
-// tiles (and last, partial tile) waste the fewest lanes; ties to the wider tile.
+// tiles (and last, partial tile) take the least modelled time -- pass slots plus the fixed
+// cost of each tile; ties to the wider tile.
 int64_t lane_efficient_width(int64_t M, const std::vector<int>& rs, int t0, int t1, int64_t total,
                              int64_t cmax) {
   int64_t best = cmax;
-  double best_eff = -1;
+  double best_time = -1;
   for (int64_t C = cmax; C >= std::max<int64_t>(1, cmax / 2); --C) {
     double ops = 0, slots = 0;
     const int64_t full = total / C, rem = total % C;
     tile_lane_cost(C, M, rs, t0, t1, &ops, &slots);
-    ops *= (double)full;
-    slots *= (double)full;
-    if (rem) tile_lane_cost(rem, M, rs, t0, t1, &ops, &slots);
-    const double eff = slots > 0 ? ops / slots : 0;
-    if (eff > best_eff + 1e-12) {
-      best_eff = eff;
+    slots = (slots + kTileOverheadOps) * (double)full;
+    if (rem) {
+      tile_lane_cost(rem, M, rs, t0, t1, &ops, &slots);
+      slots += kTileOverheadOps;
+    }
+    if (best_time < 0 || slots < best_time - 1e-9) {
+      best_time = slots;
       best = C;
     }
   }
@@ -241,7 +252,7 @@ std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt) {
       g2.out_elem = P;
       g1.total_sub = Q;
       g2.total_sub = P;
-      if (!r.per_size_mode) {   // tile widths that leave the fewest warp lanes idle
+      if (!r.per_size_mode) {   // tile widths with the least modelled pass time
         for (GroupDesc* g : {&g1, &g2}) {
           int64_t cmax = std::max<int64_t>(1, opt.tile_target / g->M);
           while (cmax > 1 && !ragged_tile_fits(cmax, g->M)) --cmax;

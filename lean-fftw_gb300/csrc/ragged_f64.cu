@@ -39,7 +39,11 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Request a tile of C sub-problems of group g, starting at sub-problem s0, from `src` into
-// stage buffer X (padded tile layout), with the element order of copy_tile's loads.
+// stage buffer X (padded tile layout), with the element order of copy_tile's loads:
+// consecutive threads take consecutive elements of a sub-problem when those are contiguous
+// (in_elem == 1), else neighbouring sub-problems.  Each thread walks its elements with
+// running (sub-problem, element) indices -- one division per tile, not three per element --
+// and a tile inside one line (every tile of a two-group item) reads that line's base once.
 template <class Lines>
 __device__ __forceinline__ void stage_tile(double2* X, const GroupDesc& g, const Lines& lines,
                                            int64_t s0, int C, const double2* src) {
@@ -54,22 +58,60 @@ __device__ __forceinline__ void stage_tile(double2* X, const GroupDesc& g, const
   const bool elem_fast = elem_st == 1;
   const int64_t line0 = s0 / nsub;
   const int sub0 = (int)(s0 - line0 * nsub);
-  const int nn = elem_fast ? C * M : gC * M;
   const int PM = sub_pitch(M);
-  for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
-    int c, i;
-    if (elem_fast) {
-      c = fdiv(idx, fd_m);
-      i = idx - c * M;
-    } else {
-      i = fdiv(idx, fd_c);
-      c = idx - i * gC;
-      if (c >= C) continue;
+  const int S = blockDim.x;
+  if (elem_fast) {
+    // idx = c * M + i over the C sub-problems present
+    const int nn = C * M;
+    int c = fdiv(threadIdx.x, fd_m);
+    int i = threadIdx.x - c * M;
+    const int dc = fdiv(S, fd_m), di = S - dc * M;
+    for (int idx = threadIdx.x; idx < nn; idx += S) {
+      const int t = sub0 + c;
+      const int ql = fdiv(t, fd_nsub);
+      const int64_t a = L.in(line0 + ql) + (int64_t)(t - ql * nsub) * sub_st + i;
+      cp_async16(X + c * PM + spad(i), src + a);
+      c += dc;
+      i += di;
+      if (i >= M) {
+        i -= M;
+        ++c;
+      }
     }
-    const int t = sub0 + c;
-    const int ql = fdiv(t, fd_nsub);
-    const int64_t a = L.in(line0 + ql) + (int64_t)(t - ql * nsub) * sub_st + (int64_t)i * elem_st;
-    cp_async16(X + c * PM + spad(i), src + a);
+  } else {
+    // idx = i * gC + c over the full tile width (a partial tile skips the missing columns)
+    const int nn = gC * M;
+    int i = fdiv(threadIdx.x, fd_c);
+    int c = threadIdx.x - i * gC;
+    const int di = fdiv(S, fd_c), dc = S - di * gC;
+    if (sub0 + C <= nsub) {
+      // one line: its base once, then (sub0 + c) * sub_st + i * elem_st
+      const double2* base = src + L.in(line0) + (int64_t)sub0 * sub_st;
+      for (int idx = threadIdx.x; idx < nn; idx += S) {
+        if (c < C) cp_async16(X + c * PM + spad(i), base + (int64_t)c * sub_st + (int64_t)i * elem_st);
+        c += dc;
+        i += di;
+        if (c >= gC) {
+          c -= gC;
+          ++i;
+        }
+      }
+    } else {
+      for (int idx = threadIdx.x; idx < nn; idx += S) {
+        if (c < C) {
+          const int t = sub0 + c;
+          const int ql = fdiv(t, fd_nsub);
+          const int64_t a = L.in(line0 + ql) + (int64_t)(t - ql * nsub) * sub_st + (int64_t)i * elem_st;
+          cp_async16(X + c * PM + spad(i), src + a);
+        }
+        c += dc;
+        i += di;
+        if (c >= gC) {
+          c -= gC;
+          ++i;
+        }
+      }
+    }
   }
   cp_async_commit();
 }

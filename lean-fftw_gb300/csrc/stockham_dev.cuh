@@ -259,33 +259,59 @@ __device__ __forceinline__ void copy_tile(typename Prec<T>::C* tile, const typen
   const int64_t line0 = s0 / nsub;
   const int sub0 = (int)(s0 - line0 * nsub);
   // strided sub-problems: neighbouring threads take neighbouring sub-problems, over the full
-  // tile width g.C (a partial last tile skips the missing columns)
+  // tile width g.C (a partial last tile skips the missing columns).  Each thread walks its
+  // elements with running (sub-problem, element) indices -- one division per tile -- and a
+  // tile inside one line reads that line's base once.
   const int nn = elem_fast ? n : gC * M;
   const bool unit = g.unit_scale != 0;
   const T sc = sizeof(T) == 4 ? (T)g.scale_f32 : (T)g.scale;
   const int PM = sub_pitch(M);
-  for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
-    int c, i;
-    if (elem_fast) {
-      c = fdiv(idx, fd_m);
-      i = idx - c * M;
-    } else {
-      i = fdiv(idx, fd_c);
-      c = idx - i * gC;
-      if (c >= C) continue;
+  const int S = blockDim.x;
+  int c, i, dc, di;
+  if (elem_fast) {
+    c = fdiv(threadIdx.x, fd_m);
+    i = threadIdx.x - c * M;
+    dc = fdiv(S, fd_m);
+    di = S - dc * M;
+  } else {
+    i = fdiv(threadIdx.x, fd_c);
+    c = threadIdx.x - i * gC;
+    di = fdiv(S, fd_c);
+    dc = S - di * gC;
+  }
+  const bool one_line = sub0 + C <= nsub;
+  const int64_t base0 = one_line ? (LOAD ? L.in(line0) : L.out(line0)) + (int64_t)sub0 * sub_st : 0;
+  for (int idx = threadIdx.x; idx < nn; idx += S) {
+    if (c < C) {
+      int64_t a;
+      if (one_line) {
+        a = base0 + (int64_t)c * sub_st + (int64_t)i * elem_st;
+      } else {
+        const int t = sub0 + c;
+        const int ql = fdiv(t, fd_nsub);
+        const int64_t line = line0 + ql;
+        const int64_t sub = t - ql * nsub;
+        a = (LOAD ? L.in(line) : L.out(line)) + sub * sub_st + (int64_t)i * elem_st;
+      }
+      if (LOAD) {
+        tile[c * PM + spad(i)] = gin[a];
+      } else if (unit) {
+        gout[a] = tile[c * PM + spad(i)];
+      } else {
+        const auto v = tile[c * PM + spad(i)];
+        gout[a] = P::mk(P::mul(v.x, sc), P::mul(v.y, sc));
+      }
     }
-    const int t = sub0 + c;
-    const int ql = fdiv(t, fd_nsub);
-    const int64_t line = line0 + ql;
-    const int64_t sub = t - ql * nsub;
-    const int64_t a = (LOAD ? L.in(line) : L.out(line)) + sub * sub_st + (int64_t)i * elem_st;
-    if (LOAD) {
-      tile[c * PM + spad(i)] = gin[a];
-    } else if (unit) {
-      gout[a] = tile[c * PM + spad(i)];
-    } else {
-      const auto v = tile[c * PM + spad(i)];
-      gout[a] = P::mk(P::mul(v.x, sc), P::mul(v.y, sc));
+    c += dc;
+    i += di;
+    if (elem_fast) {
+      if (i >= M) {
+        i -= M;
+        ++c;
+      }
+    } else if (c >= gC) {
+      c -= gC;
+      ++i;
     }
   }
 }

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "stockham_dev.cuh"
 
@@ -71,6 +72,113 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
   return false;
 }
 
+// ---- pass policies of the persistent kernel ------------------------------------------------
+
+// Any plan: the runtime pass descriptors of the group (stockham_dev.cuh).  Pass 0 reads the
+// unpadded stage buffer a bulk copy filled.
+struct GenericPasses {
+  template <bool FWD>
+  static __device__ __forceinline__ void pass(int t, const float2* src, float2* dst, int C,
+                                              const GroupDesc& g) {
+    if (t == 0) run_pass_t<float, FWD, false>(src, dst, C, g.M, g.pass[t], -1, g.nsub, g.fd_nsub);
+    else run_pass_t<float, FWD>(src, dst, C, g.M, g.pass[t], -1, g.nsub, g.fd_nsub);
+  }
+};
+
+// One pass of a one-group power-of-two plan with compile-time geometry: sub-problems of M
+// points, radix R, NS = product of the earlier radices (also the twiddle rows' length, a
+// single group's table index being k).  The same codelet on the same operands as the generic
+// pass, so the same bits; what the constants remove is index arithmetic: divisions by M/R and
+// NS become shifts and masks, and the padded shared-memory addresses of a butterfly's inputs
+// and outputs become one base plus immediate offsets wherever the stride in r is a multiple
+// of 16 (spad(x + 16 m) = spad(x) + 17 m).
+template <bool FWD, int M, int R, int NS, bool SRCPAD>
+__device__ __forceinline__ void pass_pow2(const float2* __restrict__ src, float2* __restrict__ dst,
+                                          int C, const float2* __restrict__ tw) {
+  constexpr int MR = M / R;
+  constexpr int PM = sub_pitch(M);
+  constexpr bool TW = NS > 1;
+  static_assert((M & (M - 1)) == 0 && (R & (R - 1)) == 0 && M % R == 0, "power-of-two pass");
+  const int nb = C * MR;
+  const float one = 1.0f, nz = -0.0f;   // (the binary32 codelets do not use them)
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+    const int c = q / MR;
+    const int j = q % MR;
+    float x[TW ? 4 * R - 2 : 2 * R];
+    float y[2 * R];
+    const float2* sc = src + c * (SRCPAD ? PM : M);
+    if (SRCPAD && MR % 16 == 0) {
+      const float2* s0 = sc + spad(j);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float2 v = s0[r * (MR + MR / 16)];
+        x[2 * r] = v.x;
+        x[2 * r + 1] = v.y;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int si = j + r * MR;
+        const float2 v = sc[SRCPAD ? spad(si) : si];
+        x[2 * r] = v.x;
+        x[2 * r + 1] = v.y;
+      }
+    }
+    const int b = j / NS;
+    const int k = j % NS;
+    if (TW) {
+      const float2* __restrict__ w = tw + k;
+#pragma unroll
+      for (int r = 0; r < R - 1; ++r) {
+        const float2 v = __ldg(w + r * NS);
+        x[2 * R + 2 * r] = v.x;
+        x[2 * R + 2 * r + 1] = v.y;
+      }
+    }
+    BflyF<FWD, R, TW>::run(x, y, one, nz);
+    const int d0 = b * NS * R + k;
+    float2* dc = dst + c * PM;
+    if (NS % 16 == 0) {
+      float2* o = dc + spad(d0);
+#pragma unroll
+      for (int r = 0; r < R; ++r) o[r * (NS + NS / 16)] = make_float2(y[2 * r], y[2 * r + 1]);
+    } else if (NS == 1 && R == 16) {
+      float2* o = dc + 17 * b;   // outputs 16 b .. 16 b + 15: spad(16 b + r) = 17 b + r
+#pragma unroll
+      for (int r = 0; r < R; ++r) o[r] = make_float2(y[2 * r], y[2 * r + 1]);
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) dc[spad(d0 + r * NS)] = make_float2(y[2 * r], y[2 * r + 1]);
+    }
+  }
+}
+
+// A one-group power-of-two plan with radices R0, R1, R2, R3 (0: no such pass), M points.
+template <int M, int R0, int R1, int R2, int R3>
+struct Pow2Passes {
+  template <bool FWD>
+  static __device__ __forceinline__ void pass(int t, const float2* src, float2* dst, int C,
+                                              const GroupDesc& g) {
+    switch (t) {
+      case 0:
+        pass_pow2<FWD, M, R0, 1, false>(src, dst, C, nullptr);
+        break;
+      case 1:
+        if constexpr (R1 > 0)
+          pass_pow2<FWD, M, R1, R0, true>(src, dst, C, static_cast<const float2*>(g.pass[1].tw));
+        break;
+      case 2:
+        if constexpr (R2 > 0)
+          pass_pow2<FWD, M, R2, R0 * R1, true>(src, dst, C, static_cast<const float2*>(g.pass[2].tw));
+        break;
+      default:
+        if constexpr (R3 > 0)
+          pass_pow2<FWD, M, R3, R0 * R1 * R2, true>(src, dst, C, static_cast<const float2*>(g.pass[3].tw));
+        break;
+    }
+  }
+};
+
 // Persistent binary32 kernel for back-to-back lines of one pass group: each CTA walks the
 // tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...; the bulk-copy engine prefetches kStages
 // tiles ahead into stage buffers (one mbarrier each) while the CTA runs the passes of the
@@ -79,7 +187,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
 // A wait that gives up sets *status = 1, waits (bounded) for this CTA's copies in flight and
 // returns.  tile_limit bounds the tile waits (kSpinLimit; 0 in tests of the give-up path, whose
 // drain still uses kSpinLimit).
-template <bool FWD>
+template <bool FWD, class Passes = GenericPasses>
 __global__ void __launch_bounds__(kGroupThreads, 3)
 stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __restrict__ out,
                   int64_t lines, int* status, uint32_t tile_limit) {
@@ -124,8 +232,7 @@ stream_kernel_f32(const GroupDesc g, const float2* __restrict__ in, float2* __re
     float2* src = smem_f32s + s * CM;
     float2* dst = A;
     for (int t = 0; t < g.npass; ++t) {
-      if (t == 0) run_pass_t<float, FWD, false>(src, dst, C, M, g.pass[t], -1, g.nsub, g.fd_nsub);
-      else run_pass_t<float, FWD>(src, dst, C, M, g.pass[t], -1, g.nsub, g.fd_nsub);
+      Passes::template pass<FWD>(t, src, dst, C, g);
       __syncthreads();
       if (t == 0) {
         // the stage buffer has been read: refill it with this CTA's tile kStages ahead
@@ -262,14 +369,63 @@ cudaError_t allow_max_smem(K kern) {
                               (int)(kMaxSmemBytes - a.sharedSizeBytes));
 }
 
+using StreamFn = void (*)(const GroupDesc, const float2*, float2*, int64_t, int*, uint32_t);
+
+// The persistent kernel of plan variant v: -1 = any plan (runtime pass descriptors), else the
+// power-of-two plan kPow2Plans[v] with compile-time passes.
+template <bool FWD>
+StreamFn stream_fn(int v) {
+  switch (v) {
+    case 0: return stream_kernel_f32<FWD, Pow2Passes<16, 16, 0, 0, 0>>;
+    case 1: return stream_kernel_f32<FWD, Pow2Passes<32, 16, 2, 0, 0>>;
+    case 2: return stream_kernel_f32<FWD, Pow2Passes<64, 16, 4, 0, 0>>;
+    case 3: return stream_kernel_f32<FWD, Pow2Passes<128, 16, 8, 0, 0>>;
+    case 4: return stream_kernel_f32<FWD, Pow2Passes<256, 16, 16, 0, 0>>;
+    case 5: return stream_kernel_f32<FWD, Pow2Passes<512, 16, 16, 2, 0>>;
+    case 6: return stream_kernel_f32<FWD, Pow2Passes<1024, 16, 16, 4, 0>>;
+    case 7: return stream_kernel_f32<FWD, Pow2Passes<2048, 16, 16, 8, 0>>;
+    case 8: return stream_kernel_f32<FWD, Pow2Passes<4096, 16, 16, 16, 0>>;
+    case 9: return stream_kernel_f32<FWD, Pow2Passes<8192, 16, 16, 16, 2>>;
+    default: return stream_kernel_f32<FWD, GenericPasses>;
+  }
+}
+
+// The (size, radices) of the compile-time variants above, in the same order.
+struct Pow2Plan {
+  int n;
+  int r[4];
+};
+constexpr Pow2Plan kPow2Plans[] = {
+    {16, {16, 0, 0, 0}},    {32, {16, 2, 0, 0}},    {64, {16, 4, 0, 0}},
+    {128, {16, 8, 0, 0}},   {256, {16, 16, 0, 0}},  {512, {16, 16, 2, 0}},
+    {1024, {16, 16, 4, 0}}, {2048, {16, 16, 8, 0}}, {4096, {16, 16, 16, 0}},
+    {8192, {16, 16, 16, 2}}};
+constexpr int kPow2Variants = (int)(sizeof(kPow2Plans) / sizeof(kPow2Plans[0]));
+
 }  // namespace
+
+int stream_variant_f32(int64_t n, const std::vector<int>& rs) {
+  for (int v = 0; v < kPow2Variants; ++v) {
+    const Pow2Plan& p = kPow2Plans[v];
+    if (p.n != n) continue;
+    size_t np = 0;
+    while (np < 4 && p.r[np] > 0) ++np;
+    if (np != rs.size()) return -1;
+    for (size_t t = 0; t < np; ++t)
+      if (p.r[t] != rs[t]) return -1;
+    return v;
+  }
+  return -1;
+}
 
 cudaError_t prepare_group_kernels_f32() {
   cudaError_t e = allow_max_smem(group_kernel_f32<true>);
   if (e != cudaSuccess) return e;
   if ((e = allow_max_smem(group_kernel_f32<false>)) != cudaSuccess) return e;
-  if ((e = allow_max_smem(stream_kernel_f32<true>)) != cudaSuccess) return e;
-  if ((e = allow_max_smem(stream_kernel_f32<false>)) != cudaSuccess) return e;
+  for (int v = -1; v < kPow2Variants; ++v) {
+    if ((e = allow_max_smem(stream_fn<true>(v))) != cudaSuccess) return e;
+    if ((e = allow_max_smem(stream_fn<false>(v))) != cudaSuccess) return e;
+  }
   if ((e = allow_max_smem(tile_stream_kernel_f32<true>)) != cudaSuccess) return e;
   return allow_max_smem(tile_stream_kernel_f32<false>);
 }
@@ -303,9 +459,9 @@ size_t stream_smem_bytes_f32(const GroupDesc& g) {
   return ((size_t)kStages * g.C * g.M + 2 * (size_t)tile_elems(g.C, g.M)) * sizeof(float2);
 }
 
-int stream_blocks_per_sm_f32(const GroupDesc& g) {
+int stream_blocks_per_sm_f32(const GroupDesc& g, int variant) {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_kernel_f32<true>, kGroupThreads,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, stream_fn<true>(variant), kGroupThreads,
                                                     stream_smem_bytes_f32(g)) != cudaSuccess)
     return 1;
   return nb > 0 ? nb : 1;
@@ -313,11 +469,12 @@ int stream_blocks_per_sm_f32(const GroupDesc& g) {
 
 cudaError_t launch_stream_f32(const GroupDesc& gd, bool fwd, const void* in, void* out,
                               int64_t lines, unsigned grid, int* status, cudaStream_t stream,
-                              bool give_up) {
+                              bool give_up, int variant) {
   GroupDesc g = gd;
   set_divisors(g);
   if (lines <= 0) return cudaSuccess;
-  auto kern = fwd ? stream_kernel_f32<true> : stream_kernel_f32<false>;
+  if (variant >= kPow2Variants) variant = -1;
+  const StreamFn kern = fwd ? stream_fn<true>(variant) : stream_fn<false>(variant);
   kern<<<grid, kGroupThreads, stream_smem_bytes_f32(g), stream>>>(
       g, static_cast<const float2*>(in), static_cast<float2*>(out), lines, status,
       give_up ? 0u : kSpinLimit);

@@ -58,6 +58,30 @@ def test_fp32_inplace_and_unaligned():
     assert torch.equal(un_out.view(B, n), plan.execute(shifted))
 
 
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("n", [1 << k for k in range(4, 14)])
+def test_power_of_two_variants_equal_generic_passes(n, sign):
+    """One-group power-of-two plans run a persistent kernel whose passes are compiled for the
+    plan (shifts, masks and immediate offsets instead of runtime index arithmetic).  A buffer
+    offset by one complex value (not 16-byte aligned) takes the generic kernel with runtime
+    pass descriptors: both must give the same bits."""
+    B = max(3, min(64, (1 << 16) // n)) + 1
+    x = O.uniform_complex((B + 1, n), seed=n + sign).astype(np.complex64)
+    plan = lfg.plan_1d(n, sign, B, precision="f32")
+    aligned = torch.from_numpy(x[:B].copy()).cuda()
+    fast = plan.execute(aligned)
+    buf = torch.from_numpy(x.reshape(-1)).cuda()
+    un_out = torch.empty(B * n + 1, dtype=torch.complex64, device="cuda")[1:]
+    plan.execute(buf[1: 1 + B * n], un_out)                     # 8-byte offset: generic
+    shifted = torch.from_numpy(x.reshape(-1)[1: 1 + B * n].reshape(B, n)).cuda()
+    fast_shifted = plan.execute(shifted)                         # aligned copy: variant
+    torch.cuda.synchronize()
+    assert torch.equal(un_out.view(B, n), fast_shifted), n
+    ref = O.dd_dft(sign < 0, x[:B].astype(np.complex128), nthreads=8)
+    e = O.rel_l2(fast.cpu().numpy().astype(np.complex128), ref)
+    assert e < 4 * U32 * max(1.0, np.sqrt(np.log2(n))), (n, e)
+
+
 @pytest.mark.parametrize("n", [1 << 16, 1 << 17, 1 << 18])
 def test_compensation_helps_large_sizes(n):
     """Compensated (hi, lo) twiddle products in the last passes remove the twiddles' own
