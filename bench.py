@@ -36,7 +36,9 @@ itself, Lean 4 + AVX-512 assembly, cannot be built or run on this aarch64 host),
 threads, one transform per thread, on a bounded sample of the same workload.
 
 Multi-GPU: transforms are independent, so N ranks each run the full per-GPU batch with no
-collective (weak scaling); the barrier and max-over-ranks timing follow torchrun's env.
+collective (weak scaling); the barrier and max-over-ranks timing follow torchrun's env.  With
+--shard the ranks split one ragged batch instead (lfg.shard_ragged: cost-balanced, the same
+split computed on every rank; strong scaling).
 """
 from __future__ import annotations
 
@@ -588,6 +590,9 @@ def main():
                     choices=sorted(WORKLOADS) + ["fp64_peak", "precision"])
     ap.add_argument("--impl", default="lfg", choices=["lfg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--shard", action="store_true",
+                    help="ragged, N > 1: split the one batch over the ranks (lfg.shard_ragged, "
+                         "cost-balanced) instead of a full batch per rank (strong scaling)")
     ap.add_argument("--untuned", action="store_true",
                     help="ragged: plan with the default schedule instead of autotuning it "
                          "(profiling runs, where the tuner's candidate launches would be captured)")
@@ -631,8 +636,14 @@ def main():
     rng = np.random.default_rng(rank_seed(rank))
     extra = {}
     out_shape, out_dtype, alg_bytes_override = None, None, None
+    job_flops = None      # whole-job flops per step when the ranks split one batch
     if wl["kind"] == "ragged":
         sizes = ragged_workload_sizes(wl)
+        if args.shard and ws > 1:
+            shard, _ = lfg.shard_ragged(sizes, ws)
+            job_flops = float(sum(flops_per_transform(int(n)) for n in sizes))
+            sizes = sizes[shard == rank]
+            extra["shard"] = {"ranks": ws, "transforms_this_rank": int(sizes.size)}
         total = int(sizes.sum())
         t_plan = time.perf_counter()
         plan = lfg.plan_ragged(sizes, wl["sign"], measure=not args.untuned)   # autotuned
@@ -724,7 +735,10 @@ def main():
     # headline: device-resident inputs
     ms, clocks = timed(step_fn, args.steps, stream, local, barrier, flush)
     ms = max_over_ranks(ms, dev)
-    value = flops_step * ws / (ms * 1e-3) / 1e9
+    scaling = "weak" if job_flops is None else "strong"
+    if job_flops is None:
+        job_flops = flops_step * ws
+    value = job_flops / (ms * 1e-3) / 1e9
 
     if wl["kind"] == "ragged":
         # the comparison point: one launch per distinct size, in one chain (each size after
@@ -737,7 +751,7 @@ def main():
             ps_ms, _ = timed(ps_step, min(20, max(5, args.steps // 4)), stream, local, barrier)
             ps_ms = max_over_ranks(ps_ms, dev)
             torch.cuda.synchronize()
-            extra[key] = {"value": round(flops_step * ws / (ps_ms * 1e-3) / 1e9, 3),
+            extra[key] = {"value": round(job_flops / (ps_ms * 1e-3) / 1e9, 3),
                           "unit": "GFLOP/s", "ms_per_step": round(ps_ms, 4),
                           "launches_per_step": int(ps_plan.info().launches),
                           "speedup_of_persistent": round(ps_ms / ms, 3),
@@ -770,7 +784,7 @@ def main():
     for _ in range(e2e_steps):
         host_fn(hin_np, hout_np)
     t_e2e = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dev)
-    e2e = flops_step * ws / t_e2e / 1e9
+    e2e = job_flops / t_e2e / 1e9
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -783,12 +797,12 @@ def main():
         config.update(extra.pop("config_extra"))
         config["l2_flush"] = ("inputs larger than L2 (129 MB)" if flush is None else
                               "L2 flushed before every timed step (258 MB write, not timed)")
-        config["parallelism"] = f"replicas{ws}"
+        config["parallelism"] = f"replicas{ws}" if scaling == "weak" else f"shards{ws}"
         metric = metric_name(wl)
         line = {
             "metric": metric, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "higher_is_better": True, "scaling": scaling, "vs_baseline": None,
             "dtype": wl.get("precision", "f64"),
             "data": "synthetic", "config": config,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,

@@ -242,6 +242,15 @@ size_t lfg_wisdom_count(void);
 lfg_status lfg_plan_layout(size_t n, lfg_precision precision, int *radices, int *npass,
                            int *first_group);
 
+/* Split a ragged batch over nshards devices (no counterpart in the reference, which runs one
+ * transform at a time on one host): transform i goes to shard[i] in 0..nshards-1, balancing
+ * each shard's codelet operations (the binary64 kernels are bound by them; sizes outside the
+ * fast engine count 5 n log2 n), largest transforms first.  Host only, deterministic, so every
+ * rank computes the same split from the same sizes.  cost (nshards doubles, may be NULL)
+ * receives each shard's operations. */
+lfg_status lfg_shard_ragged(const int64_t *sizes, size_t count, int nshards, int *shard,
+                            double *cost);
+
 /* Human-readable text of a status, and the last error message of this thread. */
 const char *lfg_strerror(lfg_status s);
 const char *lfg_last_error(void);

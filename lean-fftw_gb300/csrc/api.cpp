@@ -8,6 +8,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <exception>
+#include <map>
 #include <new>
 #include <string>
 
@@ -1340,6 +1341,41 @@ static lfg_status lfg_plan_layout_impl(size_t n, lfg_precision precision, int* r
   return LFG_OK;
 }
 
+static lfg_status lfg_shard_ragged_impl(const int64_t* sizes, size_t count, int nshards,
+                                        int* shard, double* cost) {
+  if ((!sizes || !shard) && count) return fail(LFG_ERR_INVALID, "null array");
+  if (nshards < 1) return fail(LFG_ERR_INVALID, "nshards must be >= 1");
+  // cost of a transform: its codelet operations (the binary64 kernels are bound by them);
+  // sizes the fast engine does not cover count 5 n log2 n
+  std::vector<double> c(count);
+  std::map<int64_t, double> memo;
+  for (size_t i = 0; i < count; ++i) {
+    const int64_t n = sizes[i];
+    if (n < 1) return fail(LFG_ERR_INVALID, "sizes must be >= 1");
+    auto it = memo.find(n);
+    if (it == memo.end()) {
+      double v = 5.0 * (double)n * std::log2((double)std::max<int64_t>(2, n));
+      if (n >= 2 && n <= ((int64_t)1 << 24) && smooth13(n))
+        v = lfg::plan_ops(n, lfg::choose_radices(n, 0));
+      it = memo.emplace(n, v).first;
+    }
+    c[i] = it->second;
+  }
+  // longest processing time first: each transform, largest first (ties by index), to the
+  // least loaded shard (ties to the lower shard) -- deterministic on every rank
+  std::vector<size_t> order(count);
+  for (size_t i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return c[a] > c[b]; });
+  std::vector<double> load(nshards, 0.0);
+  for (size_t i : order) {
+    const int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    shard[i] = s;
+    load[s] += c[i];
+  }
+  if (cost) std::copy(load.begin(), load.end(), cost);
+  return LFG_OK;
+}
+
 static lfg_status lfg_wisdom_import_impl(const char* path) {
   if (!path) return fail(LFG_ERR_INVALID, "null path");
   if (!lfg::wisdom_import(path)) return fail(LFG_ERR_INVALID, std::string("cannot read ") + path);
@@ -1447,6 +1483,11 @@ lfg_status lfg_get_ragged_radices(const lfg_ragged* plan, int64_t n, int* radice
 
 lfg_status lfg_cos_sin_table(uint64_t n, double* out) {
   return guarded([&] { return lfg_cos_sin_table_impl(n, out); });
+}
+
+lfg_status lfg_shard_ragged(const int64_t* sizes, size_t count, int nshards, int* shard,
+                            double* cost) {
+  return guarded([&] { return lfg_shard_ragged_impl(sizes, count, nshards, shard, cost); });
 }
 
 lfg_status lfg_plan_layout(size_t n, lfg_precision precision, int* radices, int* npass,

@@ -44,9 +44,11 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // (in_elem == 1), else neighbouring sub-problems.  Each thread walks its elements with
 // running (sub-problem, element) indices -- one division per tile, not three per element --
 // and a tile inside one line (every tile of a two-group item) reads that line's base once.
+// The copies are spread over threads tid = 0 .. S-1 of the calling subset (all the CTA's
+// threads, or the warps without work in the pass that runs meanwhile).
 template <class Lines>
 __device__ __forceinline__ void stage_tile(double2* X, const GroupDesc& g, const Lines& lines,
-                                           int64_t s0, int C, const double2* src) {
+                                           int64_t s0, int C, const double2* src, int tid, int S) {
   // descriptor fields in registers: each cp.async below is a compiler memory barrier, after
   // which fields read through a reference would be loaded again for every element
   const int64_t sub_st = g.in_sub, elem_st = g.in_elem;
@@ -59,14 +61,13 @@ __device__ __forceinline__ void stage_tile(double2* X, const GroupDesc& g, const
   const int64_t line0 = s0 / nsub;
   const int sub0 = (int)(s0 - line0 * nsub);
   const int PM = sub_pitch(M);
-  const int S = blockDim.x;
   if (elem_fast) {
     // idx = c * M + i over the C sub-problems present
     const int nn = C * M;
-    int c = fdiv(threadIdx.x, fd_m);
-    int i = threadIdx.x - c * M;
+    int c = fdiv(tid, fd_m);
+    int i = tid - c * M;
     const int dc = fdiv(S, fd_m), di = S - dc * M;
-    for (int idx = threadIdx.x; idx < nn; idx += S) {
+    for (int idx = tid; idx < nn; idx += S) {
       const int t = sub0 + c;
       const int ql = fdiv(t, fd_nsub);
       const int64_t a = L.in(line0 + ql) + (int64_t)(t - ql * nsub) * sub_st + i;
@@ -81,13 +82,13 @@ __device__ __forceinline__ void stage_tile(double2* X, const GroupDesc& g, const
   } else {
     // idx = i * gC + c over the full tile width (a partial tile skips the missing columns)
     const int nn = gC * M;
-    int i = fdiv(threadIdx.x, fd_c);
-    int c = threadIdx.x - i * gC;
+    int i = fdiv(tid, fd_c);
+    int c = tid - i * gC;
     const int di = fdiv(S, fd_c), dc = S - di * gC;
     if (sub0 + C <= nsub) {
       // one line: its base once, then (sub0 + c) * sub_st + i * elem_st
       const double2* base = src + L.in(line0) + (int64_t)sub0 * sub_st;
-      for (int idx = threadIdx.x; idx < nn; idx += S) {
+      for (int idx = tid; idx < nn; idx += S) {
         if (c < C) cp_async16(X + c * PM + spad(i), base + (int64_t)c * sub_st + (int64_t)i * elem_st);
         c += dc;
         i += di;
@@ -97,7 +98,7 @@ __device__ __forceinline__ void stage_tile(double2* X, const GroupDesc& g, const
         }
       }
     } else {
-      for (int idx = threadIdx.x; idx < nn; idx += S) {
+      for (int idx = tid; idx < nn; idx += S) {
         if (c < C) {
           const int t = sub0 + c;
           const int ql = fdiv(t, fd_nsub);
@@ -152,16 +153,16 @@ struct TaskIO {
   double2* mine;
 
   __device__ __forceinline__ void stage(double2* X, const RaggedClass& rc, const RaggedItem& w,
-                                        const Task& t) const {
+                                        const Task& t, int tid, int S) const {
     const GroupDesc& g = rc.g[t.grp];
     if (rc.ngroups == 1 || (!mine && t.grp == 0)) {
-      stage_tile(X, g, ListedLines{in_off, out_off, w.first}, t.s0, t.C, in);
+      stage_tile(X, g, ListedLines{in_off, out_off, w.first}, t.s0, t.C, in, tid, S);
     } else if (!mine) {
-      stage_tile(X, g, ListedLines{out_off, out_off, w.first}, t.s0, t.C, out);
+      stage_tile(X, g, ListedLines{out_off, out_off, w.first}, t.s0, t.C, out, tid, S);
     } else if (t.grp == 0) {
-      stage_tile(X, g, FixedBases{__ldg(in_off + w.first), 0}, t.s0, t.C, in);
+      stage_tile(X, g, FixedBases{__ldg(in_off + w.first), 0}, t.s0, t.C, in, tid, S);
     } else {
-      stage_tile(X, g, FixedBases{0, 0}, t.s0, t.C, mine);
+      stage_tile(X, g, FixedBases{0, 0}, t.s0, t.C, mine, tid, S);
     }
   }
 
@@ -246,7 +247,7 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
     for (int k = 0; k < nt; ++k) {
       const Task t = task_of(rc, w, k);
       const GroupDesc& g = rc.g[t.grp];
-      if (!staged) io.stage(X, rc, w, t);
+      if (!staged) io.stage(X, rc, w, t, threadIdx.x, NT);
       cp_async_wait_all();
       __syncthreads();   // X complete for every thread
       const int sub0 = g.twsub ? (int)(t.s0 % g.nsub) : -1;
@@ -258,16 +259,29 @@ ragged_kernel_f64(const RaggedClass* __restrict__ classes, const RaggedItem* __r
       __syncthreads();   // X consumed; s_next visible
       if (k == 0) next = s_next;
       staged = false;
+      // who requests the next tile: when the next pass leaves two or more warps without a
+      // butterfly, those warps do, while the others run the pass (the copies' address
+      // arithmetic then overlaps the FP64 work); otherwise every thread, before the pass
+      int s_tid = threadIdx.x, s_n = NT;
+      if (np > 1) {
+        const int busy = ((t.C * (g.M / g.pass[1].R) + 31) / 32) * 32;
+        if (busy <= NT - 64) {
+          s_tid = (int)threadIdx.x - busy;
+          s_n = NT - busy;
+        }
+      }
       if (k + 1 < nt) {
         const Task tn = task_of(rc, w, k + 1);
         if (tn.grp == t.grp) {
-          io.stage(X, rc, w, tn);
+          if (s_tid >= 0) io.stage(X, rc, w, tn, s_tid, s_n);
           staged = true;
         }
       } else if (next < nitems) {
-        const RaggedItem wn = items[next];
-        const RaggedClass& rn = classes[wn.cls];
-        io.stage(X, rn, wn, task_of(rn, wn, 0));
+        if (s_tid >= 0) {
+          const RaggedItem wn = items[next];
+          const RaggedClass& rn = classes[wn.cls];
+          io.stage(X, rn, wn, task_of(rn, wn, 0), s_tid, s_n);
+        }
         staged = true;
       }
       double2* A = Y;

@@ -76,6 +76,9 @@ _SIG = {
     "lfg_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "lfg_last_error": (ctypes.c_char_p, []),
     "lfg_cos_sin_table": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]),
+    "lfg_shard_ragged": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64), ctypes.c_size_t,
+                                        ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(ctypes.c_double)]),
     "lfg_plan_layout": (ctypes.c_int, [ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "lfg_wisdom_import": (ctypes.c_int, [ctypes.c_char_p]),

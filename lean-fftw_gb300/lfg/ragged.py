@@ -162,3 +162,17 @@ def ragged_sizes(count: int = 8192, seed: int = 20261016, lo: int = 2, hi: int =
     i = np.clip(np.searchsorted(L, u), 1, len(S) - 1)
     left = u - L[i - 1] <= L[i] - u
     return np.where(left, S[i - 1], S[i]).astype(np.int64)
+
+
+def shard_ragged(sizes: Sequence[int], nshards: int):
+    """Split a ragged batch over `nshards` devices (lfg_shard_ragged): returns (shard, cost),
+    shard[i] the device of transform i, cost[s] the codelet operations of device s.  The
+    split balances those operations, largest transforms first, and is deterministic, so every
+    rank of a job computes the same one; rank r then plans `sizes[shard == r]`."""
+    s = np.ascontiguousarray(sizes, dtype=np.int64)
+    shard = np.empty(s.size, dtype=np.int32)
+    cost = np.empty(int(nshards), dtype=np.float64)
+    check(lib().lfg_shard_ragged(s.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), s.size,
+                                 int(nshards), shard.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                 cost.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return shard, cost

@@ -45,3 +45,25 @@ def test_bench_workloads_match_the_configurations():
     assert W["large_262144_f32"]["precision"] == "f32"
     assert (W["r2c_512x512"]["n0"], W["r2c_512x512"]["n1"], W["r2c_512x512"]["batch"]) == (512, 512, 64)
     assert np.array_equal(b.ragged_workload_sizes(W["ragged"]), np.sort(lfg.ragged_sizes(8192)))
+
+
+def test_shard_ragged_balances_and_covers():
+    """lfg.shard_ragged splits the benchmark's ragged batch over 2..8 devices: every transform
+    exactly once, shard costs equal to the sum of their transforms' codelet operations, and the
+    largest shard within 1 % of the mean (host only, no GPU)."""
+    import lfg
+    from lfg.codegen.plans import choose_radices
+    from lfg.codegen.kernel import butterfly_k
+    sizes = lfg.ragged_sizes(8192)
+    ops = {}
+    for n in set(sizes.tolist()):
+        rs = choose_radices(n)
+        ops[n] = sum((n // R) * sum(butterfly_k(True, R, t > 0).counts()) for t, R in enumerate(rs))
+    for k in (2, 3, 4, 8):
+        shard, cost = lfg.shard_ragged(sizes, k)
+        assert shard.min() >= 0 and shard.max() < k
+        for s in range(k):
+            assert cost[s] == sum(ops[int(n)] for n in sizes[shard == s])
+        assert cost.max() <= 1.01 * cost.mean(), (k, cost)
+    again, _ = lfg.shard_ragged(sizes, 4)
+    assert (again == lfg.shard_ragged(sizes, 4)[0]).all()
