@@ -48,6 +48,9 @@ typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
  * once (its bulk copies still land and are waited for before the kernel exits).  A call on
  * such a plan computes nothing useful; lfg_device_status then returns LFG_ERR_TIMEOUT. */
 #define LFG_TEST_WAIT_GIVE_UP 32u
+/* Run the kernels with runtime pass descriptors even where a kernel compiled for the plan's
+ * geometry exists (binary32 power-of-two plans): the same bits, for comparing the two. */
+#define LFG_GENERIC_KERNELS 128u
 
 typedef struct lfg_plan lfg_plan;
 
@@ -164,6 +167,7 @@ typedef struct {
   int64_t in_bytes;     /* spanned input bytes per execution                 */
   int64_t out_bytes;    /* spanned output bytes per execution                */
   double flops;         /* binary64 instructions of the codelets per execution */
+  int cluster_ctas;     /* a lone transform on a thread-block cluster: its CTAs (0: none) */
 } lfg_plan_info;
 
 lfg_status lfg_get_plan_info(const lfg_plan *plan, lfg_plan_info *info);

@@ -175,7 +175,12 @@ lfg_status build_c2c_device(lfg::Plan& p) {
     return build_chirp_device(p);
   }
   // binary64 is bound by the FP64 pipe: two groups of small tiles (more CTAs per SM) beat one
-  // group with a CTA-sized tile above 2048 points; binary32 is bound by HBM: as few groups as fit
+  // group with a CTA-sized tile above 2048 points; binary32 is bound by HBM: as few groups as fit.
+  // A lone contiguous binary64 transform of up to kClusterMaxN points stays one group, which
+  // the thread-block cluster kernel runs.
+  if (p.single_max == 0 && p.precision == 0 && p.howmany == 1 && p.howmany2 == 1 &&
+      p.n <= lfg::kClusterMaxN && p.in.stride == 1 && p.out.stride == 1)
+    p.single_max = lfg::kClusterMaxN;
   if (p.single_max == 0 && p.precision == 0) p.single_max = single_max_default();
   if (p.single_max == 0 && p.precision == 1) p.single_max = lfg::kF32SingleGroupMax;
   int dev = 0;
@@ -412,11 +417,15 @@ lfg_status plan_1d_common(size_t n, int sign, size_t howmany, lfg_precision prec
   p.empty = howmany == 0;
   p.no_comp = (flags & LFG_NO_COMPENSATION) != 0;
   p.wait_give_up = (flags & LFG_TEST_WAIT_GIVE_UP) != 0;
+  p.generic_kernels = (flags & LFG_GENERIC_KERNELS) != 0;
   p.measure = (flags & LFG_MEASURE) != 0 && !radices;
   if (radices) {
     if (npass < 1 || npass > lfg::kMaxPass) return fail(LFG_ERR_INVALID, "bad pass count");
     p.radices.assign(radices, radices + npass);
     p.radices_given = true;
+  } else if (howmany == 1 && precision == LFG_F64 && p.n <= lfg::kClusterMaxN && !p.measure) {
+    // a lone transform runs on a thread-block cluster: the radices of least latency
+    p.radices = lfg::choose_radices_latency(p.n);
   } else {
     p.radices = lfg::choose_radices(p.n, precision);
   }
@@ -1121,6 +1130,7 @@ static lfg_status lfg_get_plan_info_impl(const lfg_plan* plan, lfg_plan_info* in
   info->in_bytes = p.in_span * (p.precision == 0 ? 8 : 4);
   info->out_bytes = p.out_span * (p.precision == 0 ? 8 : 4);
   info->flops = p.flops;
+  info->cluster_ctas = p.cluster ? lfg::cluster_size_f64(p.groups[0]) : 0;
   return LFG_OK;
 }
 

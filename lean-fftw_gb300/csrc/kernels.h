@@ -39,12 +39,24 @@ cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void
 // size n with radices rs, or -1.
 int stream_variant_f32(int64_t n, const std::vector<int>& rs);
 
+// One binary64 transform of N <= kClusterMaxN points (one group, contiguous line) spread over a
+// thread-block cluster of cluster_size_f64(g) CTAs (the latency path of a lone transform);
+// tw_base / tw_len: the plan's whole twiddle table (interleaved pairs), copied into each CTA.
+constexpr int kClusterMaxN = 4096;
+int cluster_size_f64(const GroupDesc& g);
+size_t cluster_smem_bytes_f64(const GroupDesc& g, int tw_len);
+cudaError_t launch_cluster_f64(const GroupDesc& g, bool fwd, const void* in, void* out,
+                               const void* tw_base, int tw_len, cudaStream_t stream);
+
 // Persistent FP32 kernel for tiles of strided sub-problems (three tile buffers: a stage
 // filled by asynchronous element copies, two work buffers); in and out 8-byte aligned.
-size_t tile_stream_smem_bytes_f32(const GroupDesc& g);
-int tile_stream_blocks_per_sm_f32(const GroupDesc& g);
+// variant: -1 for any group, or tile_variant_f32's index of a group of a two-group power-of-two
+// plan compiled with its passes as constants (the same bits, less index arithmetic).
+size_t tile_stream_smem_bytes_f32(const GroupDesc& g, int variant = -1);
+int tile_stream_blocks_per_sm_f32(const GroupDesc& g, int variant = -1);
+int tile_variant_f32(const GroupDesc& g);
 cudaError_t launch_tile_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
-                                   unsigned grid, cudaStream_t stream);
+                                   unsigned grid, cudaStream_t stream, int variant = -1);
 
 // Persistent FP64 kernel over a ragged batch (one launch for all sizes), in kRaggedVariants
 // block shapes (threads x minimum CTAs per SM).

@@ -85,13 +85,18 @@ struct Plan {
   bool stream = false;
   unsigned stream_grid = 0;
   int stream_variant = -1;      // compile-time power-of-two variant of that kernel (-1: none)
+  // a lone binary64 transform of at most kClusterMaxN points runs on a thread-block cluster
+  bool cluster = false;
+  int cluster_tw_len = 0;       // complex entries of the plan's twiddle table
   // binary32 groups not covered by the stream kernel: the persistent strided-tile kernel
   // (asynchronous copies of the next tile), one grid per group
   bool tile_stream = false;
   unsigned ts_grid[2] = {0, 0};
+  int ts_variant[2] = {-1, -1};  // compile-time two-group power-of-two variants (-1: none)
   unsigned col_ts_grid = 0;     // binary32 column pass of a rank-2 real plan: persistent grid
   int* d_status = nullptr; // set to 1 on the device when a bounded wait gave up
   bool wait_give_up = false;  // LFG_TEST_WAIT_GIVE_UP: tile waits give up at once (tests)
+  bool generic_kernels = false;  // LFG_GENERIC_KERNELS: no compile-time kernel variants
   // real transforms (kind R2C / C2R): rows of the last dimension, and for rank 2 the complex
   // transform along the first dimension (columns of the half spectrum)
   RealDesc real{};
@@ -138,6 +143,9 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target);
 // Radix sequence with the fewest codelet operations for size n (first pass untwiddled),
 // or an empty vector when n is not 13-smooth.
 std::vector<int> choose_radices(int64_t n, int precision);
+// Radix sequence of least latency for one transform of size n on a thread-block cluster
+// (each pass costs one butterfly's operations per thread plus a fixed pass cost), or empty.
+std::vector<int> choose_radices_latency(int64_t n);
 // The fewest-operation radices of each factor of the most balanced split n = P * Q (larger
 // factor first), so split_point cuts at P; empty if n is prime or not 13-smooth.
 std::vector<int> balanced_radices(int64_t n);

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <map>
 
 #include "generated/opcounts.h"
@@ -111,6 +112,53 @@ std::vector<int> choose_radices(int64_t n, int precision) {
     if (c < best - 1e-12 || (std::fabs(c - best) <= 1e-12 && t.seq.size() + 1 < seq.size())) {
       best = c;
       seq = t.seq;
+      seq.insert(seq.begin(), R0);
+    }
+  }
+  return seq;
+}
+
+std::vector<int> choose_radices_latency(int64_t n) {
+  // a pass of a lone transform costs the serial binary64 operations of one butterfly (each
+  // warp instruction holds its sub-partition's FP64 pipe for 64 cycles, so butterflies on
+  // other warps are free) times the butterflies per thread (1024 threads at most), plus the
+  // pass's fixed cost -- loads, distributed stores, the cluster barrier -- of kPassFixed
+  // operations' time
+  constexpr double kPassFixed = 12.0;
+  constexpr int64_t kThreads = 1024;
+  if (n < 2) return {};
+  std::map<int64_t, std::pair<double, std::vector<int>>> memo;   // twiddled tail of length m
+  std::function<const std::pair<double, std::vector<int>>&(int64_t)> tail =
+      [&](int64_t m) -> const std::pair<double, std::vector<int>>& {
+    auto it = memo.find(m);
+    if (it != memo.end()) return it->second;
+    std::pair<double, std::vector<int>> best{m == 1 ? 0.0 : INFINITY, {}};
+    if (m > 1)
+      for (int R = kMaxRadix; R >= 2; --R) {
+        if (!radix_ok(R) || m % R) continue;
+        const auto& t = tail(m / R);
+        if (!std::isfinite(t.first)) continue;
+        const double per = (double)((n / R + kThreads - 1) / kThreads);
+        const double c = kOpsTw[R] * per + kPassFixed + t.first;
+        if (c < best.first - 1e-12) {
+          best.first = c;
+          best.second = t.second;
+          best.second.insert(best.second.begin(), R);
+        }
+      }
+    return memo.emplace(m, best).first->second;
+  };
+  double best = INFINITY;
+  std::vector<int> seq;
+  for (int R0 = kMaxRadix; R0 >= 2; --R0) {
+    if (!radix_ok(R0) || n % R0) continue;
+    const auto& t = tail(n / R0);
+    if (!std::isfinite(t.first)) continue;
+    const double per = (double)((n / R0 + kThreads - 1) / kThreads);
+    const double c = kOpsUntw[R0] * per + kPassFixed + t.first;
+    if (c < best - 1e-12) {
+      best = c;
+      seq = t.second;
       seq.insert(seq.begin(), R0);
     }
   }
@@ -442,6 +490,13 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   for (int gi = 0; gi < p.ngroups; ++gi)
     for (int t = 0; t < p.groups[gi].npass; ++t)
       p.groups[gi].pass[t].comp = comp[p.group_first_pass[gi] + t];
+  // a lone binary64 transform of a contiguous line: the thread-block cluster kernel
+  p.cluster = false;
+  if (prec == 0 && p.ngroups == 1 && p.howmany == 1 && p.howmany2 == 1 && p.stages.empty() &&
+      p.in.stride == 1 && p.out.stride == 1 && cluster_size_f64(p.groups[0]) > 0) {
+    p.cluster_tw_len = (int)(pt.values.size() / 2);
+    p.cluster = cluster_smem_bytes_f64(p.groups[0], p.cluster_tw_len) <= kSmemBudget;
+  }
   // binary32 over back-to-back lines: the persistent kernel with bulk-copy prefetch
   const GroupDesc& g0 = p.groups[0];
   if (prec == 1 && p.ngroups == 1 && p.howmany2 == 1 && p.in.stride == 1 && p.out.stride == 1 &&
@@ -456,7 +511,7 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
       const int64_t tiles = (p.howmany + g0.C - 1) / g0.C;
       bool any_comp = false;
       for (int t = 0; t < g0.npass; ++t) any_comp = any_comp || g0.pass[t].comp;
-      p.stream_variant = any_comp ? -1 : stream_variant_f32(N, rs);
+      p.stream_variant = any_comp || p.generic_kernels ? -1 : stream_variant_f32(N, rs);
       const int64_t want = (int64_t)sms * stream_blocks_per_sm_f32(g0, p.stream_variant);
       p.stream_grid = (unsigned)std::max<int64_t>(1, std::min(want, tiles));
       p.stream = true;
@@ -475,9 +530,13 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
     }
     if (fits) {
       for (int gi = 0; gi < p.ngroups; ++gi) {
-        const GroupDesc& g = p.groups[gi];
+        GroupDesc& g = p.groups[gi];
+        set_divisors(g);
+        int v = p.ngroups == 2 && !p.generic_kernels ? tile_variant_f32(g) : -1;
+        if (v >= 0 && tile_stream_smem_bytes_f32(g, v) > kSmemBudget) v = -1;
+        p.ts_variant[gi] = v;
         const int64_t tiles = (g.total_sub + g.C - 1) / g.C;
-        const int64_t want = (int64_t)sms * tile_stream_blocks_per_sm_f32(g);
+        const int64_t want = (int64_t)sms * tile_stream_blocks_per_sm_f32(g, v);
         p.ts_grid[gi] = (unsigned)std::max<int64_t>(1, std::min(want, tiles));
       }
       p.tile_stream = true;
@@ -734,10 +793,13 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
   auto launch = [&](int gi, const GroupDesc& g, const void* a, void* b) -> cudaError_t {
     if (p.precision == 0) return launch_group_f64(g, p.fwd, a, b, stream);
     if (p.tile_stream && ((uintptr_t)a % 8) == 0 && ((uintptr_t)b % 8) == 0)
-      return launch_tile_stream_f32(g, p.fwd, a, b, p.ts_grid[gi], stream);
+      return launch_tile_stream_f32(g, p.fwd, a, b, p.ts_grid[gi], stream, p.ts_variant[gi]);
     return launch_group_f32(g, p.fwd, a, b, stream);
   };
   if (p.ngroups == 1) {
+    if (p.cluster && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)
+      return launch_cluster_f64(p.groups[0], p.fwd, ib, ob, p.d_twiddles, p.cluster_tw_len,
+                                stream);
     // the bulk-copy engine needs 16-byte aligned ranges; in place is fine (each tile is read
     // into shared memory before it is written)
     if (p.stream && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)

@@ -66,7 +66,7 @@ struct RaggedPlan {
   mutable void* graph_out = nullptr;
 };
 
-constexpr int kPerSizeBranches = 16;
+constexpr int kPerSizeBranches = 64;
 
 std::string build_ragged(RaggedPlan& r, const RaggedOptions& opt);
 cudaError_t execute_ragged(const RaggedPlan& r, const void* in, void* out, cudaStream_t s);

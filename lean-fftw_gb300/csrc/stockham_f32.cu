@@ -318,44 +318,259 @@ __device__ __forceinline__ void load_tile_async(float2* S, const float2* in, con
   cp_async_commit();
 }
 
+// ---- tile policies of the strided-tile kernel ----------------------------------------------
+
+// Any group: runtime pass descriptors, the padded tile layout of stockham_dev.cuh.
+struct GenericTiles {
+  static __device__ __forceinline__ int pitch(const GroupDesc& g) { return sub_pitch(g.M); }
+  static __device__ __forceinline__ void load(float2* S, const float2* in, const GroupDesc& g,
+                                              int64_t s0, int C) {
+    load_tile_async(S, in, g, s0, C);
+  }
+  template <bool FWD>
+  static __device__ __forceinline__ void pass(int t, const float2* src, float2* dst, int C,
+                                              const GroupDesc& g, int sub0) {
+    run_pass_t<float, FWD>(src, dst, C, g.M, g.pass[t], sub0, g.nsub, g.fd_nsub);
+  }
+  static __device__ __forceinline__ void store(const float2* src, float2* out, const GroupDesc& g,
+                                               int64_t s0, int C) {
+    copy_tile<float, false>(const_cast<float2*>(src), nullptr, out, g,
+                            StridedLines{g.in_line, g.out_line}, s0, C);
+  }
+};
+
+// One pass of a group of a two-group power-of-two plan, compile-time geometry: sub-problems of
+// M points at pitch PM, radix R, NSL = product of the group's earlier radices; TWSUB: a second
+// group, whose table index is m * NSL + k with m = (sub0 + c) mod NSUB (rows of NSUB * NSL);
+// MODE 0 untwiddled, 1 twiddled, 2 compensated (hi, lo) twiddles -- the same operations on the
+// same operands as pass_t (stockham_dev.cuh), so the same bits.
+template <bool FWD, int M, int PM, int R, int NSL, int NSUB, bool TWSUB, int MODE>
+__device__ __forceinline__ void pass_group_pow2(const float2* __restrict__ src,
+                                                float2* __restrict__ dst, int C,
+                                                const float2* __restrict__ tw, int sub0) {
+  using P = Prec<float>;
+  constexpr int MR = M / R;
+  constexpr int NSG = TWSUB ? NSUB * NSL : NSL;
+  constexpr bool TW = MODE == 1;
+  static_assert((M & (M - 1)) == 0 && (R & (R - 1)) == 0 && (NSUB & (NSUB - 1)) == 0, "powers of two");
+  const int nb = C * MR;
+  const float one = 1.0f, nz = -0.0f;   // (the binary32 codelets do not use them)
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+    const int c = q / MR;
+    const int j = q % MR;
+    float x[TW ? 4 * R - 2 : 2 * R];
+    float y[2 * R];
+    const float2* sc = src + c * PM;
+    if (MR % 16 == 0) {
+      const float2* s0 = sc + spad(j);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float2 v = s0[r * (MR + MR / 16)];
+        x[2 * r] = v.x;
+        x[2 * r + 1] = v.y;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float2 v = sc[spad(j + r * MR)];
+        x[2 * r] = v.x;
+        x[2 * r + 1] = v.y;
+      }
+    }
+    const int b = j / NSL;
+    const int k = j % NSL;
+    const int kg = TWSUB ? ((sub0 + c) % NSUB) * NSL + k : k;
+    if (MODE == 1) {
+      const float2* __restrict__ w = tw + kg;
+#pragma unroll
+      for (int r = 0; r < R - 1; ++r) {
+        const float2 v = __ldg(w + r * NSG);
+        x[2 * R + 2 * r] = v.x;
+        x[2 * R + 2 * r + 1] = v.y;
+      }
+    } else if (MODE == 2) {
+      const float2* __restrict__ wh = tw + kg;
+      const float2* __restrict__ wl = wh + (R - 1) * NSG;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const float2 h = __ldg(wh + (r - 1) * NSG), l = __ldg(wl + (r - 1) * NSG);
+        const float wrh = h.x, wih = h.y, wrl = l.x, wil = l.y;
+        const float a = x[2 * r], bi = x[2 * r + 1];
+        const float cr = P::fma(a, wrl, -P::mul(bi, wil));
+        const float ci = P::fma(a, wil, P::mul(bi, wrl));
+        x[2 * r] = P::fma(a, wrh, P::fma(-bi, wih, cr));
+        x[2 * r + 1] = P::fma(a, wih, P::fma(bi, wrh, ci));
+      }
+    }
+    BflyF<FWD, R, TW>::run(x, y, one, nz);
+    const int d0 = b * NSL * R + k;
+    float2* dc = dst + c * PM;
+    if (NSL % 16 == 0) {
+      float2* o = dc + spad(d0);
+#pragma unroll
+      for (int r = 0; r < R; ++r) o[r * (NSL + NSL / 16)] = make_float2(y[2 * r], y[2 * r + 1]);
+    } else if (NSL == 1 && R == 16) {
+      float2* o = dc + 17 * b;
+#pragma unroll
+      for (int r = 0; r < R; ++r) o[r] = make_float2(y[2 * r], y[2 * r + 1]);
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; ++r) dc[spad(d0 + r * NSL)] = make_float2(y[2 * r], y[2 * r + 1]);
+    }
+  }
+}
+
+// A group of a two-group power-of-two plan with radices R0, R1, R2 (0: no such pass), M
+// points per sub-problem, the other group's size NSUB (a second group: TWSUB, its twiddles
+// compensated when COMP).  Tiles use an odd pitch, so the strided copies, whose neighbouring
+// threads take neighbouring sub-problems, spread over the banks; the copies walk their
+// elements with running indices.
+template <int M, int NSUB, bool TWSUB, bool COMP, int R0, int R1, int R2>
+struct Pow2GroupTiles {
+  static constexpr int PM = sub_pitch(M) | 1;
+  static constexpr int MODE_T = TWSUB ? (COMP ? 2 : 1) : 1;   // twiddled passes
+  static __device__ __forceinline__ int pitch(const GroupDesc&) { return PM; }
+  static __device__ __forceinline__ void load(float2* S, const float2* in, const GroupDesc& g,
+                                              int64_t s0, int C) {
+    // element (c, i): neighbouring threads take neighbouring sub-problems (runs of C)
+    const int gC = g.C, nsub = g.nsub;
+    const FastDiv fd_c = g.fd_c, fd_nsub = g.fd_nsub;
+    const int64_t in_line = g.in_line, in_sub = g.in_sub, in_elem = g.in_elem;
+    const int64_t line0 = s0 / nsub;
+    const int sub_0 = (int)(s0 - line0 * nsub);
+    const bool one_line = sub_0 + C <= nsub;
+    const float2* base = in + line0 * in_line + (int64_t)sub_0 * in_sub;
+    const int S_ = blockDim.x;
+    int i = fdiv(threadIdx.x, fd_c);
+    int c = (int)threadIdx.x - i * gC;
+    const int di = fdiv(S_, fd_c), dc = S_ - di * gC;
+    for (int idx = threadIdx.x; idx < gC * M; idx += S_) {
+      if (c < C) {
+        const float2* a;
+        if (one_line) {
+          a = base + (int64_t)c * in_sub + (int64_t)i * in_elem;
+        } else {
+          const int t = sub_0 + c;
+          const int ql = fdiv(t, fd_nsub);
+          a = in + (line0 + ql) * in_line + (int64_t)(t - ql * nsub) * in_sub + (int64_t)i * in_elem;
+        }
+        cp_async8(S + c * PM + spad(i), a);
+      }
+      c += dc;
+      i += di;
+      if (c >= gC) {
+        c -= gC;
+        ++i;
+      }
+    }
+    cp_async_commit();
+  }
+  template <bool FWD>
+  static __device__ __forceinline__ void pass(int t, const float2* src, float2* dst, int C,
+                                              const GroupDesc& g, int sub0) {
+    const float2* tw = static_cast<const float2*>(g.pass[t].tw);
+    switch (t) {
+      case 0:
+        pass_group_pow2<FWD, M, PM, R0, 1, NSUB, TWSUB, TWSUB ? MODE_T : 0>(src, dst, C, tw, sub0);
+        break;
+      case 1:
+        if constexpr (R1 > 0)
+          pass_group_pow2<FWD, M, PM, R1, R0, NSUB, TWSUB, MODE_T>(src, dst, C, tw, sub0);
+        break;
+      default:
+        if constexpr (R2 > 0)
+          pass_group_pow2<FWD, M, PM, R2, R0 * R1, NSUB, TWSUB, MODE_T>(src, dst, C, tw, sub0);
+        break;
+    }
+  }
+  static __device__ __forceinline__ void store(const float2* src, float2* out, const GroupDesc& g,
+                                               int64_t s0, int C) {
+    const int gC = g.C, nsub = g.nsub;
+    const FastDiv fd_c = g.fd_c, fd_nsub = g.fd_nsub;
+    const int64_t out_line = g.out_line, out_sub = g.out_sub, out_elem = g.out_elem;
+    const int64_t line0 = s0 / nsub;
+    const int sub_0 = (int)(s0 - line0 * nsub);
+    const bool unit = g.unit_scale != 0;
+    const float sc = g.scale_f32;
+    const int S_ = blockDim.x;
+    if (out_elem == 1) {
+      // contiguous sub-problems: element (c, i), neighbouring threads along i
+      int c = (int)threadIdx.x / M;
+      int i = (int)threadIdx.x - c * M;
+      const int dc = S_ / M, di = S_ - dc * M;
+      for (int idx = threadIdx.x; idx < C * M; idx += S_) {
+        const int t = sub_0 + c;
+        const int ql = fdiv(t, fd_nsub);
+        const int64_t a = (line0 + ql) * out_line + (int64_t)(t - ql * nsub) * out_sub + i;
+        const float2 v = src[c * PM + spad(i)];
+        out[a] = unit ? v : make_float2(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
+        c += dc;
+        i += di;
+        if (i >= M) {
+          i -= M;
+          ++c;
+        }
+      }
+      return;
+    }
+    int i = fdiv(threadIdx.x, fd_c);
+    int c = (int)threadIdx.x - i * gC;
+    const int di = fdiv(S_, fd_c), dc = S_ - di * gC;
+    for (int idx = threadIdx.x; idx < gC * M; idx += S_) {
+      if (c < C) {
+        const int t = sub_0 + c;
+        const int ql = fdiv(t, fd_nsub);
+        const int64_t a = (line0 + ql) * out_line + (int64_t)(t - ql * nsub) * out_sub + (int64_t)i * out_elem;
+        const float2 v = src[c * PM + spad(i)];
+        out[a] = unit ? v : make_float2(__fmul_rn(v.x, sc), __fmul_rn(v.y, sc));
+      }
+      c += dc;
+      i += di;
+      if (c >= gC) {
+        c -= gC;
+        ++i;
+      }
+    }
+  }
+};
+
 // Persistent binary32 kernel for tiles of strided sub-problems (the groups of two-group plans
 // and strided batches): each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...;
 // the next tile's elements are copied asynchronously into a stage buffer while the CTA runs
 // the later passes of the current tile and stores it, so HBM reads overlap the arithmetic
 // and the stores.  Waits are cp.async group waits (no polling).
-template <bool FWD>
+template <bool FWD, class Tiles = GenericTiles>
 __global__ void __launch_bounds__(kGroupThreads)
 tile_stream_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
   extern __shared__ __align__(16) float2 smem_ts[];
-  const int PE = (int)tile_elems(g.C, g.M);
+  const int PE = g.C * Tiles::pitch(g);
   float2* S = smem_ts;
   float2* A = S + PE;
   float2* B = A + PE;
   const int64_t ntiles = (g.total_sub + g.C - 1) / g.C;
-  const StridedLines lines{g.in_line, g.out_line};
   auto count = [&](int64_t tile) { return (int)min((int64_t)g.C, g.total_sub - tile * g.C); };
-  if ((int64_t)blockIdx.x < ntiles) load_tile_async(S, in, g, (int64_t)blockIdx.x * g.C, count(blockIdx.x));
+  if ((int64_t)blockIdx.x < ntiles) Tiles::load(S, in, g, (int64_t)blockIdx.x * g.C, count(blockIdx.x));
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t s0 = tile * g.C;
     const int C = count(tile);
     cp_async_wait_all();
     __syncthreads();
     const int sub0 = g.twsub ? (int)(s0 % g.nsub) : -1;
-    run_pass_t<float, FWD>(S, A, C, g.M, g.pass[0], sub0, g.nsub, g.fd_nsub);
+    Tiles::template pass<FWD>(0, S, A, C, g, sub0);
     __syncthreads();
     // the stage buffer has been consumed: start copying this CTA's next tile
     const int64_t next = tile + gridDim.x;
-    if (next < ntiles) load_tile_async(S, in, g, next * g.C, count(next));
+    if (next < ntiles) Tiles::load(S, in, g, next * g.C, count(next));
     float2* src = A;
     float2* dst = B;
     for (int t = 1; t < g.npass; ++t) {
-      run_pass_t<float, FWD>(src, dst, C, g.M, g.pass[t], sub0, g.nsub, g.fd_nsub);
+      Tiles::template pass<FWD>(t, src, dst, C, g, sub0);
       __syncthreads();
       float2* tmp = src;
       src = dst;
       dst = tmp;
     }
-    copy_tile<float, false>(src, nullptr, out, g, lines, s0, C);
+    Tiles::store(src, out, g, s0, C);
   }
   cp_async_wait_all();
 }
@@ -402,7 +617,66 @@ constexpr Pow2Plan kPow2Plans[] = {
     {8192, {16, 16, 16, 2}}};
 constexpr int kPow2Variants = (int)(sizeof(kPow2Plans) / sizeof(kPow2Plans[0]));
 
+using TileFn = void (*)(const GroupDesc, const float2*, float2*);
+
+// The groups of the two-group power-of-two binary32 plans (2^14 .. 2^18) with compile-time
+// passes: M, the other group's size (a second group's sub-problems per line), second group,
+// compensated twiddles, radices.  -1 = any group (runtime descriptors).
+struct TileGroup {
+  int M, nsub, twsub, comp, r[3];
+};
+constexpr TileGroup kTileGroups[] = {
+    {128, 0, 0, 0, {16, 8, 0}},    {256, 0, 0, 0, {16, 16, 0}},   {512, 0, 0, 0, {16, 16, 2}},
+    {128, 128, 1, 0, {16, 8, 0}},  {128, 256, 1, 0, {16, 8, 0}},  {256, 256, 1, 0, {16, 16, 0}},
+    {256, 256, 1, 1, {16, 16, 0}}, {512, 256, 1, 0, {2, 16, 16}}, {512, 256, 1, 1, {2, 16, 16}},
+    {512, 512, 1, 0, {16, 16, 2}}, {512, 512, 1, 1, {16, 16, 2}}};
+constexpr int kTileVariants = (int)(sizeof(kTileGroups) / sizeof(kTileGroups[0]));
+
+template <bool FWD>
+TileFn tile_fn(int v) {
+  switch (v) {
+    case 0: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<128, 1, false, false, 16, 8, 0>>;
+    case 1: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<256, 1, false, false, 16, 16, 0>>;
+    case 2: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<512, 1, false, false, 16, 16, 2>>;
+    case 3: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<128, 128, true, false, 16, 8, 0>>;
+    case 4: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<128, 256, true, false, 16, 8, 0>>;
+    case 5: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<256, 256, true, false, 16, 16, 0>>;
+    case 6: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<256, 256, true, true, 16, 16, 0>>;
+    case 7: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<512, 256, true, false, 2, 16, 16>>;
+    case 8: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<512, 256, true, true, 2, 16, 16>>;
+    case 9: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<512, 512, true, false, 16, 16, 2>>;
+    case 10: return tile_stream_kernel_f32<FWD, Pow2GroupTiles<512, 512, true, true, 16, 16, 2>>;
+    default: return tile_stream_kernel_f32<FWD, GenericTiles>;
+  }
+}
+
+// Shared memory of the strided-tile kernel: three tiles (stage and two work buffers); the
+// compile-time variants use an odd pitch.
+size_t tile_smem_bytes(const GroupDesc& g, int v) {
+  const int pitch = v >= 0 && v < kTileVariants ? (sub_pitch(g.M) | 1) : sub_pitch(g.M);
+  return 3 * (size_t)g.C * pitch * sizeof(float2);
+}
+
 }  // namespace
+
+int tile_variant_f32(const GroupDesc& g) {
+  for (int v = 0; v < kTileVariants; ++v) {
+    const TileGroup& t = kTileGroups[v];
+    if (t.M != g.M || t.twsub != g.twsub) continue;
+    if (t.twsub && t.nsub != g.nsub) continue;
+    int np = 0;
+    while (np < 3 && t.r[np] > 0) ++np;
+    if (np != g.npass) continue;
+    bool ok = true;
+    for (int p = 0; p < np && ok; ++p) {
+      ok = g.pass[p].R == t.r[p] && g.pass[p].comp == (t.twsub ? t.comp : 0);
+      // a first group's first pass is untwiddled, every other pass twiddled
+      ok = ok && ((g.pass[p].tw == nullptr) == (!t.twsub && p == 0));
+    }
+    if (ok) return v;
+  }
+  return -1;
+}
 
 int stream_variant_f32(int64_t n, const std::vector<int>& rs) {
   for (int v = 0; v < kPow2Variants; ++v) {
@@ -426,31 +700,35 @@ cudaError_t prepare_group_kernels_f32() {
     if ((e = allow_max_smem(stream_fn<true>(v))) != cudaSuccess) return e;
     if ((e = allow_max_smem(stream_fn<false>(v))) != cudaSuccess) return e;
   }
-  if ((e = allow_max_smem(tile_stream_kernel_f32<true>)) != cudaSuccess) return e;
-  return allow_max_smem(tile_stream_kernel_f32<false>);
+  for (int v = -1; v < kTileVariants; ++v) {
+    if ((e = allow_max_smem(tile_fn<true>(v))) != cudaSuccess) return e;
+    if ((e = allow_max_smem(tile_fn<false>(v))) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
-size_t tile_stream_smem_bytes_f32(const GroupDesc& g) {
-  return 3 * (size_t)tile_elems(g.C, g.M) * sizeof(float2);
+size_t tile_stream_smem_bytes_f32(const GroupDesc& g, int variant) {
+  return tile_smem_bytes(g, variant);
 }
 
-int tile_stream_blocks_per_sm_f32(const GroupDesc& g) {
+int tile_stream_blocks_per_sm_f32(const GroupDesc& g, int variant) {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tile_stream_kernel_f32<true>, kGroupThreads,
-                                                    tile_stream_smem_bytes_f32(g)) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, tile_fn<true>(variant), kGroupThreads,
+                                                    tile_smem_bytes(g, variant)) != cudaSuccess)
     return 1;
   return nb > 0 ? nb : 1;
 }
 
 cudaError_t launch_tile_stream_f32(const GroupDesc& gd, bool fwd, const void* in, void* out,
-                                   unsigned grid, cudaStream_t stream) {
+                                   unsigned grid, cudaStream_t stream, int variant) {
   GroupDesc g = gd;
   set_divisors(g);
   const int64_t ntiles = (g.total_sub + g.C - 1) / g.C;
   if (ntiles <= 0) return cudaSuccess;
+  if (variant >= kTileVariants) variant = -1;
   const unsigned gr = (unsigned)std::min<int64_t>(grid, ntiles);
-  auto kern = fwd ? tile_stream_kernel_f32<true> : tile_stream_kernel_f32<false>;
-  kern<<<gr, kGroupThreads, tile_stream_smem_bytes_f32(g), stream>>>(
+  const TileFn kern = fwd ? tile_fn<true>(variant) : tile_fn<false>(variant);
+  kern<<<gr, kGroupThreads, tile_smem_bytes(g, variant), stream>>>(
       g, static_cast<const float2*>(in), static_cast<float2*>(out));
   return cudaGetLastError();
 }

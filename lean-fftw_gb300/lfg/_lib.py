@@ -28,13 +28,16 @@ LFG_MEASURE = 1
 LFG_ADJOINT = 8
 LFG_NO_COMPENSATION = 16
 LFG_TEST_WAIT_GIVE_UP = 32
+LFG_PER_SIZE_CONCURRENT = 64
+LFG_GENERIC_KERNELS = 128
 
 
 class PlanInfo(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("howmany", ctypes.c_int64), ("sign", ctypes.c_int),
                 ("precision", ctypes.c_int), ("npass", ctypes.c_int), ("ngroups", ctypes.c_int),
                 ("radices", ctypes.c_int * 24), ("in_bytes", ctypes.c_int64),
-                ("out_bytes", ctypes.c_int64), ("flops", ctypes.c_double)]
+                ("out_bytes", ctypes.c_int64), ("flops", ctypes.c_double),
+                ("cluster_ctas", ctypes.c_int)]
 
 
 class LfgError(RuntimeError):

@@ -94,7 +94,7 @@ def _prec(precision) -> int:
 
 def plan_1d(n: int, sign: int = -1, howmany: int = 1, precision="f64",
             radices: Optional[Sequence[int]] = None, measure: bool = False,
-            compensated: bool = True) -> Plan:
+            compensated: bool = True, generic_kernels: bool = False) -> Plan:
     """1-D complex transform of size n on `howmany` contiguous lines.  Binary32 plans of
     size >= 2^16 use compensated twiddle products in their last passes unless
     compensated=False."""
@@ -104,7 +104,8 @@ def plan_1d(n: int, sign: int = -1, howmany: int = 1, precision="f64",
         check(lib().lfg_plan_1d_radices(n, sign, howmany, _prec(precision), arr, len(radices),
                                         ctypes.byref(h)))
     else:
-        flags = (LFG_MEASURE if measure else LFG_ESTIMATE) | (0 if compensated else 16)
+        flags = (LFG_MEASURE if measure else LFG_ESTIMATE) | (0 if compensated else 16) | \
+            (128 if generic_kernels else 0)
         check(lib().lfg_plan_1d(n, sign, howmany, _prec(precision), flags, ctypes.byref(h)))
     return Plan(h)
 

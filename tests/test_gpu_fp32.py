@@ -82,6 +82,27 @@ def test_power_of_two_variants_equal_generic_passes(n, sign):
     assert e < 4 * U32 * max(1.0, np.sqrt(np.log2(n))), (n, e)
 
 
+@pytest.mark.parametrize("comp", [True, False])
+@pytest.mark.parametrize("sign", [-1, 1])
+@pytest.mark.parametrize("n", [1 << k for k in range(14, 19)])
+def test_two_group_variants_equal_generic_kernels(n, sign, comp):
+    """Two-group power-of-two plans (2^14 .. 2^18) run each group on a strided-tile kernel
+    compiled for its geometry (odd tile pitch, passes with constant strides); the generic
+    kernels (LFG_GENERIC_KERNELS) must give the same bits, compensated or not."""
+    B = max(2, (1 << 20) // n)
+    x = torch.from_numpy(O.uniform_complex((B, n), seed=n + sign).astype(np.complex64)).cuda()
+    fast = lfg.plan_1d(n, sign, B, precision="f32", compensated=comp)
+    slow = lfg.plan_1d(n, sign, B, precision="f32", compensated=comp, generic_kernels=True)
+    assert fast.info().ngroups == 2
+    a, b = fast.execute(x), slow.execute(x)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b), n
+    c = x.clone()
+    fast.execute(c, c)                               # in place (through the plan's scratch)
+    torch.cuda.synchronize()
+    assert torch.equal(c, a)
+
+
 @pytest.mark.parametrize("n", [1 << 16, 1 << 17, 1 << 18])
 def test_compensation_helps_large_sizes(n):
     """Compensated (hi, lo) twiddle products in the last passes remove the twiddles' own

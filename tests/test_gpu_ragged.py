@@ -77,7 +77,7 @@ def test_ragged_benchmark_batch_full():
     torch.cuda.synchronize()
     y = yd.cpu().numpy()
     assert not _check(plan, sizes, x, y, plan.in_offsets, plan.out_offsets)
-    # per-size strategy gives the same bits, its launches in one chain or on 16 branches
+    # per-size strategy gives the same bits, its launches in one chain or on 64 branches
     for conc in (False, True):
         ps = lfg.plan_ragged(sizes, -1, per_size=True, concurrent=conc)
         y2 = torch.empty_like(xd)
