@@ -5,20 +5,30 @@
 // FP64 pipe for 64 cycles: a radix-16 pass of a 1024-point transform is 208 such instructions
 // in a row on one warp, about 6 us, whatever the other sub-partitions do.  Here a cluster of
 // S CTAs (S SMs, four warps each, one per sub-partition) shares the transform so that every
-// warp of a pass owns at most one butterfly per thread, and every CTA keeps a full copy of the
-// array in its own shared memory: a pass reads its butterflies' inputs locally and writes each
-// output into the next buffer of every CTA of the cluster (distributed shared memory), then
-// the cluster barrier orders the pass.  The passes perform the reference codelets exactly as
-// the group kernel does (same DAGs, same twiddle tables, same operand order), so the bits are
-// the same as for any other kernel of the library with the same radix sequence.
+// warp of a pass owns at most one butterfly per thread, and the planner picks radices for the
+// serial operation count of one butterfly per pass (radix 4 where the size allows).
+//
+// Data movement is kept off the critical path:
+// * the first pass reads its butterflies' inputs straight from global memory, and the last
+//   pass writes its outputs straight to global memory (no copy loops before or after);
+// * every other pass reads its inputs from this CTA's shared memory and writes each output
+//   into the shared memory of the one CTA whose thread reads it in the next pass (butterfly
+//   q of a pass runs on CTA (q / 128) mod S), then the cluster barrier orders the passes;
+// * the twiddle tables are copied into each CTA's shared memory asynchronously while the
+//   first (untwiddled) pass computes.
+// The passes perform the reference codelets exactly as the group kernel does (same DAGs,
+// same twiddle tables, same operand order), so the bits are the same as for any other kernel
+// of the library with the same radix sequence.
 //
 // The cluster barrier is a hardware barrier of co-scheduled CTAs (no polling): every thread of
 // every CTA reaches every barrier, and no CTA touches another's shared memory after the last
-// one, so none exits while its memory is still being written.
+// one, so none exits while its memory is still being written.  In place is safe: every input
+// is read in the first pass, before the barrier that precedes the first output store.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "stockham_dev.cuh"
 
@@ -30,13 +40,26 @@ namespace {
 
 constexpr int kClusterThreads = 128;   // one warp per SM sub-partition
 
-// One pass over the whole transform: butterflies q = q0, q0 + qstep, ... of N / R, inputs from
-// the local buffer `src` (padded layout spad), twiddles from the local table copy, outputs to
-// the same position of the next buffer in every CTA of the cluster.
-template <bool FWD, int R, bool TW, int S>
-__device__ __forceinline__ void cluster_pass(const double2* __restrict__ src, double2* const* dst,
-                                             int N, const PassDesc& pd,
-                                             const double2* __restrict__ tw, int q0, int qstep) {
+__device__ __forceinline__ void cp_async16_cl(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(dst)), "l"(src) : "memory");
+}
+
+// Pass kinds: the first pass (untwiddled; inputs from global memory, outputs to the consuming
+// CTA's buffer), a middle pass (twiddled; local buffer to the consuming CTA's buffer) and the
+// last pass (twiddled; local buffer to global memory, scaled).
+enum PassKind { kFirst = 0, kMiddle = 1, kLast = 2 };
+
+// One pass over the whole transform: butterflies q = q0, q0 + qstep, ... of N / R.  `mrn` and
+// `fdn`: butterflies per line of the next pass and its divisor (output o is read there by
+// butterfly o mod mrn).
+template <bool FWD, int R, int KIND, int S>
+__device__ __forceinline__ void cluster_pass(const double2* __restrict__ gin, const double2* src,
+                                             double2* dst, double2* __restrict__ gout, int N,
+                                             const PassDesc& pd, int mrn, FastDiv fdn,
+                                             const double2* tw, int q0, int qstep, bool unit,
+                                             double sc) {
+  constexpr bool TW = KIND != kFirst;
   const int MR = N / R;
   const int ns = pd.ns_loc;
   const int nsg = pd.ns_g;
@@ -48,7 +71,7 @@ __device__ __forceinline__ void cluster_pass(const double2* __restrict__ src, do
     double y[2 * R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const double2 v = src[spad(q + r * MR)];
+      const double2 v = KIND == kFirst ? gin[q + r * MR] : src[spad(q + r * MR)];
       x[2 * r] = v.x;
       x[2 * r + 1] = v.y;
     }
@@ -67,21 +90,37 @@ __device__ __forceinline__ void cluster_pass(const double2* __restrict__ src, do
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const double2 v = make_double2(y[2 * r], y[2 * r + 1]);
-      const int o = spad(d0 + r * ns);
-#pragma unroll
-      for (int s = 0; s < S; ++s) dst[s][o] = v;
+      const int o = d0 + r * ns;
+      if (KIND == kLast) {
+        gout[o] = unit ? v : make_double2(__dmul_rn(v.x, sc), __dmul_rn(v.y, sc));
+      } else if (S == 1) {
+        dst[spad(o)] = v;
+      } else {
+        const int qn = o - fdiv(o, fdn) * mrn;   // the next pass's butterfly reading o
+        const unsigned owner = (unsigned)(qn >> 7) & (unsigned)(S - 1);
+        *cg::this_cluster().map_shared_rank(dst + spad(o), owner) = v;
+      }
     }
   }
 }
 
 template <bool FWD, int S>
-__device__ __forceinline__ void cluster_pass_any(const double2* src, double2* const* dst, int N,
-                                                 const PassDesc& pd, const double2* tw, int q0,
-                                                 int qstep) {
-#define LFG_CPASS(RR)                                                              \
-  case RR:                                                                         \
-    if (tw) cluster_pass<FWD, RR, true, S>(src, dst, N, pd, tw, q0, qstep);        \
-    else cluster_pass<FWD, RR, false, S>(src, dst, N, pd, tw, q0, qstep);          \
+__device__ __forceinline__ void cluster_pass_any(int kind, const double2* gin, const double2* src,
+                                                 double2* dst, double2* gout, int N,
+                                                 const PassDesc& pd, int mrn, FastDiv fdn,
+                                                 const double2* tw, int q0, int qstep, bool unit,
+                                                 double sc) {
+#define LFG_CPASS(RR)                                                                          \
+  case RR:                                                                                     \
+    if (kind == kFirst)                                                                        \
+      cluster_pass<FWD, RR, kFirst, S>(gin, src, dst, gout, N, pd, mrn, fdn, tw, q0, qstep,    \
+                                       unit, sc);                                              \
+    else if (kind == kMiddle)                                                                  \
+      cluster_pass<FWD, RR, kMiddle, S>(gin, src, dst, gout, N, pd, mrn, fdn, tw, q0, qstep,   \
+                                        unit, sc);                                             \
+    else                                                                                       \
+      cluster_pass<FWD, RR, kLast, S>(gin, src, dst, gout, N, pd, mrn, fdn, tw, q0, qstep,     \
+                                      unit, sc);                                               \
     break;
   switch (pd.R) {
     LFG_CPASS(2)
@@ -115,41 +154,37 @@ cluster_kernel_f64(const GroupDesc g, const double2* in, double2* out,
   const int N = g.M;
   const int PN = sub_pitch(N);
   const int rank = (int)cluster.block_rank();
-  double2* A = smem_cl;
-  double2* B = smem_cl + PN;
   double2* T = smem_cl + 2 * PN;
-  // the input line and the twiddle tables, into this CTA's shared memory (in == out is
-  // allowed: every CTA has read the input before the first barrier, and the output is
-  // written after the last)
-  for (int i = threadIdx.x; i < N; i += blockDim.x) A[spad(i)] = in[i];
-  for (int i = threadIdx.x; i < tw_len; i += blockDim.x) T[i] = tw_base[i];
-  // the same buffers in every CTA of the cluster
-  double2* dA[S];
-  double2* dB[S];
-#pragma unroll
-  for (int s = 0; s < S; ++s) {
-    dA[s] = cluster.map_shared_rank(A, s);
-    dB[s] = cluster.map_shared_rank(B, s);
-  }
-  cluster.sync();   // every copy loaded before any remote write
+  // the twiddle tables arrive while the first pass computes (it needs none)
+  for (int i = threadIdx.x; i < tw_len; i += blockDim.x) cp_async16_cl(T + i, tw_base + i);
+  asm volatile("cp.async.commit_group;" ::: "memory");
   const int q0 = rank * kClusterThreads + threadIdx.x;
   const int qstep = S * kClusterThreads;
-  bool in_a = true;
-  for (int t = 0; t < g.npass; ++t) {
+  const bool unit = g.unit_scale != 0;
+  const double sc = g.scale;
+  const int last = g.npass - 1;
+  for (int t = 0; t <= last; ++t) {
     const PassDesc& pd = g.pass[t];
     const double2* tw = pd.tw ? T + (static_cast<const double2*>(pd.tw) - tw_base) : nullptr;
-    cluster_pass_any<FWD, S>(in_a ? A : B, in_a ? dB : dA, N, pd, tw, q0, qstep);
-    cluster.sync();   // the pass's outputs are in every CTA before the next pass reads them
-    in_a = !in_a;
+    // a one-pass transform writes its buffer and stores it below (in place stays safe)
+    const int kind = t == 0 ? kFirst : (t == last ? kLast : kMiddle);
+    const PassDesc& pn = g.pass[t < last ? t + 1 : t];
+    // pass t writes buffer t mod 2 and reads the other one
+    double2* const wbuf = smem_cl + ((t & 1) ? PN : 0);
+    const double2* const rbuf = smem_cl + ((t & 1) ? 0 : PN);
+    cluster_pass_any<FWD, S>(kind, in, rbuf, wbuf, out, N, pd, N / pn.R, pn.fd_mr, tw, q0,
+                             qstep, unit, sc);
+    if (t < last || last == 0) {
+      if (t == 0) asm volatile("cp.async.wait_group 0;" ::: "memory");
+      cluster.sync();   // this pass's outputs are in place before the next pass reads them
+    }
   }
-  // every CTA holds the whole result: each stores its share
-  const double2* res = in_a ? A : B;
-  const int per = (N + S - 1) / S;
-  const int lo = rank * per, hi = min(N, lo + per);
-  const double sc = g.scale;
-  for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
-    const double2 v = res[spad(i)];
-    out[i] = g.unit_scale ? v : make_double2(__dmul_rn(v.x, sc), __dmul_rn(v.y, sc));
+  if (last == 0) {   // S == 1: the buffer holds the whole result
+    const double2* res = smem_cl;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      const double2 v = res[spad(i)];
+      out[i] = unit ? v : make_double2(__dmul_rn(v.x, sc), __dmul_rn(v.y, sc));
+    }
   }
 }
 
@@ -157,8 +192,18 @@ template <bool FWD, int S>
 cudaError_t launch_s(const GroupDesc& g, const void* in, void* out, const double2* tw_base,
                      int tw_len, size_t smem, cudaStream_t stream) {
   auto kern = cluster_kernel_f64<FWD, S>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the shared-memory opt-in once per device (devices 0..63)
+  static std::atomic<unsigned long long> opted{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev < 64 ? 1ull << dev : 0;
+  if (!bit || !(opted.load(std::memory_order_relaxed) & bit)) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(kSmemBudget));
+    if (e != cudaSuccess) return e;
+    opted.fetch_or(bit, std::memory_order_relaxed);
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(S, 1, 1);
   cfg.blockDim = dim3(kClusterThreads, 1, 1);
@@ -183,7 +228,8 @@ int cluster_size_f64(const GroupDesc& g) {
   for (int t = 0; t < g.npass; ++t) widest = std::max(widest, g.M / g.pass[t].R);
   int S = 1;
   while (S < 8 && S * kClusterThreads < widest) S *= 2;
-  return S;
+  // a one-pass transform stores from its own buffer: one CTA
+  return g.npass == 1 && S > 1 ? 0 : S;
 }
 
 size_t cluster_smem_bytes_f64(const GroupDesc& g, int tw_len) {

@@ -93,6 +93,10 @@ struct Plan {
   bool tile_stream = false;
   unsigned ts_grid[2] = {0, 0};
   int ts_variant[2] = {-1, -1};  // compile-time two-group power-of-two variants (-1: none)
+  // binary32 two-group plans over contiguous lines: the register-staged kernel of each group
+  // (direct_f32.cu; -1: none).  Set for both groups or neither; the second group's twiddle
+  // tables are then in pass order rather than transposed.
+  int direct_variant[2] = {-1, -1};
   unsigned col_ts_grid = 0;     // binary32 column pass of a rank-2 real plan: persistent grid
   int* d_status = nullptr; // set to 1 on the device when a bounded wait gave up
   bool wait_give_up = false;  // LFG_TEST_WAIT_GIVE_UP: tile waits give up at once (tests)

@@ -431,7 +431,22 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   PassTables pt = make_pass_tables(N, p.fwd, rs, prec);
   const std::vector<int> comp = compensated_passes(N, rs, split, p.no_comp ? 0 : prec);
   if (prec == 1) pt.values = split_compensated(pt, rs, comp);
-  transpose_second_group(pt, rs, split, comp);
+  // binary32 two-group plans over contiguous lines whose two groups both have a
+  // register-staged kernel: the second group reads its tables in pass order
+  p.direct_variant[0] = p.direct_variant[1] = -1;
+  if (prec == 1 && split > 0 && split < (int)rs.size() && !p.generic_kernels &&
+      p.howmany2 == 1 && p.in.stride == 1 && p.out.stride == 1) {
+    int64_t P = 1;
+    for (int t = 0; t < split; ++t) P *= rs[t];
+    const int v1 = direct_variant_f32((int)P, (int)(N / P), false, false, rs.data(), split);
+    const int v2 = direct_variant_f32((int)(N / P), (int)P, true, comp[split] != 0,
+                                      rs.data() + split, (int)rs.size() - split);
+    if (v1 >= 0 && v2 >= 0) {
+      p.direct_variant[0] = v1;
+      p.direct_variant[1] = v2;
+    }
+  }
+  if (p.direct_variant[1] < 0) transpose_second_group(pt, rs, split, comp);
   interleave_tables(pt, rs, comp);
   p.d_twiddles = upload_tables(pt.values, prec, &msg);
   if (!p.d_twiddles) return msg;
@@ -792,6 +807,8 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
   char* ob = static_cast<char*>(out) + p.out.offset * (int64_t)es;
   auto launch = [&](int gi, const GroupDesc& g, const void* a, void* b) -> cudaError_t {
     if (p.precision == 0) return launch_group_f64(g, p.fwd, a, b, stream);
+    // (its tables are laid out for it: no other kernel may run this group)
+    if (p.direct_variant[gi] >= 0) return launch_direct_f32(g, p.fwd, a, b, p.direct_variant[gi], stream);
     if (p.tile_stream && ((uintptr_t)a % 8) == 0 && ((uintptr_t)b % 8) == 0)
       return launch_tile_stream_f32(g, p.fwd, a, b, p.ts_grid[gi], stream, p.ts_variant[gi]);
     return launch_group_f32(g, p.fwd, a, b, stream);

@@ -86,14 +86,18 @@ def test_power_of_two_variants_equal_generic_passes(n, sign):
 @pytest.mark.parametrize("sign", [-1, 1])
 @pytest.mark.parametrize("n", [1 << k for k in range(14, 19)])
 def test_two_group_variants_equal_generic_kernels(n, sign, comp):
-    """Two-group power-of-two plans (2^14 .. 2^18) run each group on a strided-tile kernel
-    compiled for its geometry (odd tile pitch, passes with constant strides); the generic
-    kernels (LFG_GENERIC_KERNELS) must give the same bits, compensated or not."""
+    """Two-group power-of-two plans run each group on a kernel compiled for its geometry: the
+    register-staged two-pass kernel up to 2^16 (first pass from global memory, last pass to
+    global memory, second-group tables in pass order), the strided-tile kernel with constant
+    strides above; the generic kernels (LFG_GENERIC_KERNELS) must give the same bits,
+    compensated or not, out of place (the intermediate in the output) and in place."""
     B = max(2, (1 << 20) // n)
     x = torch.from_numpy(O.uniform_complex((B, n), seed=n + sign).astype(np.complex64)).cuda()
     fast = lfg.plan_1d(n, sign, B, precision="f32", compensated=comp)
     slow = lfg.plan_1d(n, sign, B, precision="f32", compensated=comp, generic_kernels=True)
     assert fast.info().ngroups == 2
+    assert fast.info().direct_groups == (2 if n <= 1 << 16 else 0)
+    assert slow.info().direct_groups == 0
     a, b = fast.execute(x), slow.execute(x)
     torch.cuda.synchronize()
     assert torch.equal(a, b), n
