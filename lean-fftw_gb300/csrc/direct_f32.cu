@@ -1,25 +1,25 @@
-// Binary32 groups of two-group power-of-two plans over contiguous lines, staged through
-// registers instead of copy loops.
+// Binary32 groups over contiguous lines, staged through registers instead of copy loops.
 //
 // A two-group plan of N = P * Q points runs its first passes as Q sub-problems of P points
 // (sub-problem b reads x[b + Q i], writes the row z[b P + m]) and its last passes as P
 // sub-problems of Q points (sub-problem m reads the column z[i P + m], writes the column
-// out[o P + m]).  Each CTA here takes one tile of C neighbouring sub-problems (4096 points,
-// 16 per thread) and runs the group's two passes:
-// * the first pass loads its butterflies' inputs straight from global memory into registers,
-//   neighbouring threads on neighbouring sub-problems (runs of C contiguous elements), and
-//   writes its outputs to one shared-memory tile (odd pitch: conflict-free across
-//   sub-problems);
-// * after one barrier the second pass reads the tile and stores its outputs straight to
-//   global memory: along the row (neighbouring threads on neighbouring outputs) for a first
-//   group, across sub-problems (runs of C) for a second group.
-// No element passes through a copy loop, and there is one barrier per tile.  Latency is
-// hidden by occupancy (several CTAs per SM) and by the sixteen independent loads of each
-// thread's first butterfly.
+// out[o P + m]); a one-group plan runs whole lines (rows in, rows out).  Each CTA here takes
+// one tile of C neighbouring sub-problems (4096 points, 16 per thread) and runs the group's
+// two or three passes:
+// * the first pass loads its butterflies' inputs straight from global memory into registers
+//   -- neighbouring threads on neighbouring sub-problems for columns (runs of C contiguous
+//   elements), on neighbouring elements for rows -- and writes its outputs to a shared tile;
+// * a middle pass goes from one shared tile to the other;
+// * the last pass reads a shared tile and stores its outputs straight to global memory:
+//   along the row (neighbouring threads on neighbouring outputs) or across sub-problems.
+// No element passes through a copy loop, and there is one barrier per pass boundary.  The
+// tile pitch is chosen per tile width so that the passes that walk across sub-problems hit
+// distinct banks.  Latency is hidden by occupancy (three CTAs per SM) and by the independent
+// loads of each thread's first butterflies.
 //
 // The butterflies perform the same operations on the same operands as every other binary32
 // kernel of the library (the generated codelets, the same twiddle values and compensated
-// products), so the bits are the same.  The second group's twiddle tables are kept in pass
+// products), so the bits are the same.  A second group's twiddle tables are kept in pass
 // order (index k P + m: the sub-problem index fastest), which neighbouring threads read as
 // contiguous runs.
 #include <cuda_runtime.h>
@@ -34,40 +34,68 @@ namespace {
 constexpr int kDirectThreads = 256;
 constexpr int kDirectPoints = 4096;   // points per tile
 
-enum DirectTarget { kToTile = 0, kToRows = 1, kToCols = 2 };
+// Global layouts of a group's sub-problems (element i of sub-problem c of the tile):
+//   kFirstOfTwo   in c + i NSUB (columns), out c M + i (rows)
+//   kSecondOfTwo  in columns, out c + i NSUB (columns)
+//   kSingle       in c LDI + i, out c LDO + i (rows at the plan's line distances)
+constexpr int kFirstOfTwo = kDirectFirstOfTwo;
+constexpr int kSecondOfTwo = kDirectSecondOfTwo;
+constexpr int kSingle = kDirectSingle;
+enum DirectSrc { kFromTile = 0, kFromCols = 1, kFromRows = 2 };
+enum DirectDst { kToTile = 0, kToRows = 1, kToCols = 2 };
 
-// One pass of a group with compile-time geometry: sub-problems of M points, tile of C
-// sub-problems at pitch PM, radix R, NSL = product of the group's earlier radices, NSUB = the
-// other group's size; TWSUB: a second group (twiddle index k * NSUB + m); MODE 0 untwiddled,
-// 1 twiddled, 2 compensated (hi, lo) twiddles.  FROM_GLOBAL: inputs from the tile's first
-// column element `gin` (element (c, i) at gin[c + i NSUB]), else from the shared tile.
-template <bool FWD, int M, int C, int R, int NSL, int NSUB, bool TWSUB, int MODE, bool FROM_GLOBAL,
-          int TO>
-__device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, const float2* src,
-                                            float2* dst, float2* __restrict__ gout,
-                                            const float2* __restrict__ tw, int sub0, bool unit,
-                                            float sc) {
+// Tile pitch: odd for tiles of 16 or more sub-problems, 2 mod 16 for 8 (a half-warp then
+// spans 8 sub-problems and two neighbouring elements), the padded length otherwise (those
+// passes walk along the sub-problem).
+LFG_HD constexpr int direct_pitch(int M, int C) {
+  return C >= 16 ? (sub_pitch(M) | 1) : (C == 8 ? sub_pitch(M) + ((2 - sub_pitch(M)) & 15) : sub_pitch(M));
+}
+
+// One pass with compile-time geometry: sub-problems of M points, tile of C sub-problems at
+// pitch PM, radix R, NSL = product of the group's earlier radices, NSUB = the other group's
+// size; TWSUB: a second group (twiddle index k * NSUB + m); MODE 0 untwiddled, 1 twiddled,
+// 2 compensated (hi, lo) twiddles.  `gin` / `gout`: the tile's first element in global
+// memory; ldi / ldo: line distances of rows; count: sub-problems of the tile present (rows
+// only; the others are never loaded or stored).
+template <bool FWD, int M, int C, int PM, int R, int NSL, int NSUB, bool TWSUB, int MODE, int SRC,
+          int DST>
+__device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, int64_t ldi,
+                                            const float2* src, float2* dst,
+                                            float2* __restrict__ gout, int64_t ldo,
+                                            const float2* __restrict__ tw, int sub0, int count,
+                                            bool unit, float sc) {
   using P = Prec<float>;
-  constexpr int PM = sub_pitch(M) | 1;
   constexpr int MR = M / R;
   constexpr int NB = C * MR;
   constexpr int NSG = TWSUB ? NSUB * NSL : NSL;
   constexpr bool TW = MODE == 1;
-  constexpr bool JFAST = TO == kToRows;   // row stores: neighbouring threads along the row
+  // across sub-problems where a column is read or written and for a second group's passes
+  // (its twiddles are contiguous across sub-problems), along them where a row is
+  constexpr bool CFAST = (SRC == kFromCols || DST == kToCols || TWSUB) && SRC != kFromRows &&
+                         DST != kToRows;
   static_assert(NB % kDirectThreads == 0, "whole butterflies per thread");
   const float one = 1.0f, nz = -0.0f;   // (the binary32 codelets do not use them)
 #pragma unroll
   for (int it = 0; it < NB / kDirectThreads; ++it) {
     const int q = (int)threadIdx.x + it * kDirectThreads;
-    const int c = JFAST ? q / MR : q % C;
-    const int j = JFAST ? q % MR : q / C;
+    const int c = CFAST ? q % C : q / MR;
+    const int j = CFAST ? q / C : q % MR;
     float x[TW ? 4 * R - 2 : 2 * R];
     float y[2 * R];
-    if (FROM_GLOBAL) {
+    if (SRC == kFromCols) {
       const float2* s = gin + c + j * NSUB;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const float2 v = s[r * MR * NSUB];
+        x[2 * r] = v.x;
+        x[2 * r + 1] = v.y;
+      }
+    } else if (SRC == kFromRows) {
+      const float2* s = gin + c * ldi + j;
+      const bool present = c < count;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float2 v = present ? s[r * MR] : make_float2(0.0f, 0.0f);
         x[2 * r] = v.x;
         x[2 * r + 1] = v.y;
       }
@@ -115,7 +143,7 @@ __device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, cons
     }
     BflyF<FWD, R, TW>::run(x, y, one, nz);
     const int d0 = b * NSL * R + k;
-    if (TO == kToTile) {
+    if (DST == kToTile) {
       float2* o = dst + c * PM;
       if (NSL % 16 == 0) {
 #pragma unroll
@@ -124,50 +152,89 @@ __device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, cons
 #pragma unroll
         for (int r = 0; r < R; ++r) o[spad(d0 + r * NSL)] = make_float2(y[2 * r], y[2 * r + 1]);
       }
-    } else {
+    } else if (DST == kToCols || c < count) {
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const float2 v = unit ? make_float2(y[2 * r], y[2 * r + 1])
                               : make_float2(__fmul_rn(y[2 * r], sc), __fmul_rn(y[2 * r + 1], sc));
-        if (TO == kToRows) gout[c * M + d0 + r * NSL] = v;
+        if (DST == kToRows) gout[c * ldo + d0 + r * NSL] = v;
         else gout[c + (d0 + r * NSL) * NSUB] = v;
       }
     }
   }
 }
 
-// A two-pass group (radices R0, R1) of M points with the other group's size NSUB.
-template <bool FWD, int M, int NSUB, bool TWSUB, bool COMP, int R0, int R1>
+// A group of two or three passes (radices R0, R1, R2; R2 = 0: two) of M points; NSUB = the
+// other group's size (two-group layouts).
+template <bool FWD, int LAYOUT, int M, int NSUB, bool COMP, int R0, int R1, int R2>
 __global__ void __launch_bounds__(kDirectThreads, 3)
 direct_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
+  constexpr bool TWSUB = LAYOUT == kSecondOfTwo;
   constexpr int C = kDirectPoints / M;
-  constexpr int PM = sub_pitch(M) | 1;
+  constexpr int PM = direct_pitch(M, C);
   constexpr int MODE_T = TWSUB ? (COMP ? 2 : 1) : 1;
-  static_assert(M == R0 * R1 && NSUB % C == 0, "tile geometry");
-  __shared__ float2 tile[C * PM];
+  constexpr int SRC0 = LAYOUT == kSingle ? kFromRows : kFromCols;
+  constexpr int DSTL = LAYOUT == kSecondOfTwo ? kToCols : kToRows;
+  static_assert(M == R0 * R1 * (R2 > 0 ? R2 : 1) && C >= 1, "tile geometry");
+  extern __shared__ float2 smem_direct[];
+  float2* A = smem_direct;
+  float2* B = smem_direct + C * PM;
   const int64_t s0 = (int64_t)blockIdx.x * C;
-  const int64_t line = s0 / NSUB;
-  const int sub0 = (int)(s0 - line * NSUB);
-  const float2* gin = in + line * g.in_line + sub0;
-  float2* gout = out + line * g.out_line + (TWSUB ? (int64_t)sub0 : (int64_t)sub0 * M);
-  direct_pass<FWD, M, C, R0, 1, NSUB, TWSUB, TWSUB ? MODE_T : 0, true, kToTile>(
-      gin, nullptr, tile, nullptr, static_cast<const float2*>(g.pass[0].tw), sub0, true, 1.0f);
+  int sub0 = 0, count = C;
+  const float2* gin;
+  float2* gout;
+  int64_t ldi = M, ldo = M;
+  if (LAYOUT == kSingle) {
+    count = (int)min((int64_t)C, g.total_sub - s0);
+    gin = in + s0 * g.in_line;
+    gout = out + s0 * g.out_line;
+    ldi = g.in_line;
+    ldo = g.out_line;
+  } else {
+    const int64_t line = s0 / NSUB;
+    sub0 = (int)(s0 - line * NSUB);
+    gin = in + line * g.in_line + sub0;
+    gout = out + line * g.out_line + (TWSUB ? (int64_t)sub0 : (int64_t)sub0 * M);
+  }
+  const bool unit = g.unit_scale != 0;
+  const float sc = g.scale_f32;
+  const float2* tw0 = static_cast<const float2*>(g.pass[0].tw);
+  const float2* tw1 = static_cast<const float2*>(g.pass[1].tw);
+  direct_pass<FWD, M, C, PM, R0, 1, NSUB, TWSUB, TWSUB ? MODE_T : 0, SRC0, kToTile>(
+      gin, ldi, nullptr, A, nullptr, 0, tw0, sub0, count, true, 1.0f);
   __syncthreads();
-  direct_pass<FWD, M, C, R1, R0, NSUB, TWSUB, MODE_T, false, TWSUB ? kToCols : kToRows>(
-      nullptr, tile, nullptr, gout, static_cast<const float2*>(g.pass[1].tw), sub0,
-      g.unit_scale != 0, g.scale_f32);
+  if constexpr (R2 > 0) {
+    direct_pass<FWD, M, C, PM, R1, R0, NSUB, TWSUB, MODE_T, kFromTile, kToTile>(
+        nullptr, 0, A, B, nullptr, 0, tw1, sub0, count, true, 1.0f);
+    __syncthreads();
+    direct_pass<FWD, M, C, PM, R2, R0 * R1, NSUB, TWSUB, MODE_T, kFromTile, DSTL>(
+        nullptr, 0, B, nullptr, gout, ldo, static_cast<const float2*>(g.pass[2].tw), sub0,
+        count, unit, sc);
+  } else {
+    direct_pass<FWD, M, C, PM, R1, R0, NSUB, TWSUB, MODE_T, kFromTile, DSTL>(
+        nullptr, 0, A, nullptr, gout, ldo, tw1, sub0, count, unit, sc);
+  }
 }
 
-// The groups with a kernel here: M, the other group's size, second group, compensated
-// twiddles, radices.  They are the groups of the planner's binary32 plans of 2^14 (16.8 | 16.8),
-// 2^15 (16.16 | 16.8) and 2^16 (16.16 | 16.16, with or without compensation).
+// The groups with a kernel here: layout, M, the other group's size (1 for one group),
+// compensated twiddles, radices.  They are the groups of the planner's binary32 plans of
+// 2^9 .. 2^12 (one group) and 2^13 .. 2^18 (two groups: 16.8 | 16.4, 16.8 | 16.8,
+// 16.16 | 16.8, 16.16 | 16.16, 16.16 | 2.16.16, 16.16.2 | 16.16.2; the second groups from
+// 2^16 with and without compensation).
 struct DirectGroup {
-  int M, nsub, twsub, comp, r0, r1;
+  int layout, M, nsub, comp, r[3];
 };
 constexpr DirectGroup kDirectGroups[] = {
-    {128, 128, 0, 0, 16, 8},  {128, 128, 1, 0, 16, 8},  {256, 128, 0, 0, 16, 16},
-    {128, 256, 1, 0, 16, 8},  {256, 256, 0, 0, 16, 16}, {256, 256, 1, 1, 16, 16},
-    {256, 256, 1, 0, 16, 16}};
+    {kFirstOfTwo, 128, 128, 0, {16, 8, 0}},     {kSecondOfTwo, 128, 128, 0, {16, 8, 0}},
+    {kFirstOfTwo, 256, 128, 0, {16, 16, 0}},    {kSecondOfTwo, 128, 256, 0, {16, 8, 0}},
+    {kFirstOfTwo, 256, 256, 0, {16, 16, 0}},    {kSecondOfTwo, 256, 256, 1, {16, 16, 0}},
+    {kSecondOfTwo, 256, 256, 0, {16, 16, 0}},   {kFirstOfTwo, 256, 512, 0, {16, 16, 0}},
+    {kSecondOfTwo, 512, 256, 1, {2, 16, 16}},   {kSecondOfTwo, 512, 256, 0, {2, 16, 16}},
+    {kFirstOfTwo, 512, 512, 0, {16, 16, 2}},    {kSecondOfTwo, 512, 512, 1, {16, 16, 2}},
+    {kSecondOfTwo, 512, 512, 0, {16, 16, 2}},   {kSingle, 512, 1, 0, {16, 16, 2}},
+    {kSingle, 1024, 1, 0, {16, 16, 4}},         {kSingle, 2048, 1, 0, {16, 16, 8}},
+    {kSingle, 4096, 1, 0, {16, 16, 16}},        {kFirstOfTwo, 128, 64, 0, {16, 8, 0}},
+    {kSecondOfTwo, 64, 128, 0, {16, 4, 0}}};
 constexpr int kDirectVariants = (int)(sizeof(kDirectGroups) / sizeof(kDirectGroups[0]));
 
 using DirectFn = void (*)(const GroupDesc, const float2*, float2*);
@@ -175,28 +242,62 @@ using DirectFn = void (*)(const GroupDesc, const float2*, float2*);
 template <bool FWD>
 DirectFn direct_fn(int v) {
   switch (v) {
-    case 0: return direct_kernel_f32<FWD, 128, 128, false, false, 16, 8>;
-    case 1: return direct_kernel_f32<FWD, 128, 128, true, false, 16, 8>;
-    case 2: return direct_kernel_f32<FWD, 256, 128, false, false, 16, 16>;
-    case 3: return direct_kernel_f32<FWD, 128, 256, true, false, 16, 8>;
-    case 4: return direct_kernel_f32<FWD, 256, 256, false, false, 16, 16>;
-    case 5: return direct_kernel_f32<FWD, 256, 256, true, true, 16, 16>;
-    case 6: return direct_kernel_f32<FWD, 256, 256, true, false, 16, 16>;
+    case 0: return direct_kernel_f32<FWD, kFirstOfTwo, 128, 128, false, 16, 8, 0>;
+    case 1: return direct_kernel_f32<FWD, kSecondOfTwo, 128, 128, false, 16, 8, 0>;
+    case 2: return direct_kernel_f32<FWD, kFirstOfTwo, 256, 128, false, 16, 16, 0>;
+    case 3: return direct_kernel_f32<FWD, kSecondOfTwo, 128, 256, false, 16, 8, 0>;
+    case 4: return direct_kernel_f32<FWD, kFirstOfTwo, 256, 256, false, 16, 16, 0>;
+    case 5: return direct_kernel_f32<FWD, kSecondOfTwo, 256, 256, true, 16, 16, 0>;
+    case 6: return direct_kernel_f32<FWD, kSecondOfTwo, 256, 256, false, 16, 16, 0>;
+    case 7: return direct_kernel_f32<FWD, kFirstOfTwo, 256, 512, false, 16, 16, 0>;
+    case 8: return direct_kernel_f32<FWD, kSecondOfTwo, 512, 256, true, 2, 16, 16>;
+    case 9: return direct_kernel_f32<FWD, kSecondOfTwo, 512, 256, false, 2, 16, 16>;
+    case 10: return direct_kernel_f32<FWD, kFirstOfTwo, 512, 512, false, 16, 16, 2>;
+    case 11: return direct_kernel_f32<FWD, kSecondOfTwo, 512, 512, true, 16, 16, 2>;
+    case 12: return direct_kernel_f32<FWD, kSecondOfTwo, 512, 512, false, 16, 16, 2>;
+    case 13: return direct_kernel_f32<FWD, kSingle, 512, 1, false, 16, 16, 2>;
+    case 14: return direct_kernel_f32<FWD, kSingle, 1024, 1, false, 16, 16, 4>;
+    case 15: return direct_kernel_f32<FWD, kSingle, 2048, 1, false, 16, 16, 8>;
+    case 16: return direct_kernel_f32<FWD, kSingle, 4096, 1, false, 16, 16, 16>;
+    case 17: return direct_kernel_f32<FWD, kFirstOfTwo, 128, 64, false, 16, 8, 0>;
+    case 18: return direct_kernel_f32<FWD, kSecondOfTwo, 64, 128, false, 16, 4, 0>;
     default: return nullptr;
   }
 }
 
+size_t direct_smem(int v) {
+  const DirectGroup& d = kDirectGroups[v];
+  const int C = kDirectPoints / d.M;
+  const int tiles = d.r[2] > 0 ? 2 : 1;
+  return (size_t)tiles * C * direct_pitch(d.M, C) * sizeof(float2);
+}
+
 }  // namespace
 
-int direct_variant_f32(int M, int nsub, bool twsub, bool comp, const int* radices, int npass) {
-  if (npass != 2) return -1;
+int direct_variant_f32(int layout, int M, int nsub, bool comp, const int* radices, int npass) {
+  if (npass != 2 && npass != 3) return -1;
   for (int v = 0; v < kDirectVariants; ++v) {
     const DirectGroup& d = kDirectGroups[v];
-    if (d.M == M && d.nsub == nsub && (d.twsub != 0) == twsub && (d.comp != 0) == comp &&
-        d.r0 == radices[0] && d.r1 == radices[1])
-      return v;
+    if (d.layout != layout || d.M != M || d.nsub != nsub || (d.comp != 0) != comp) continue;
+    if ((d.r[2] > 0 ? 3 : 2) != npass) continue;
+    bool same = true;
+    for (int t = 0; t < npass; ++t) same = same && d.r[t] == radices[t];
+    if (same) return v;
   }
   return -1;
+}
+
+cudaError_t prepare_direct_kernels_f32() {
+  for (int v = 0; v < kDirectVariants; ++v) {
+    const int bytes = (int)direct_smem(v);
+    cudaError_t e = cudaFuncSetAttribute(direct_fn<true>(v),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(direct_fn<false>(v), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bytes);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_direct_f32(const GroupDesc& gd, bool fwd, const void* in, void* out,
@@ -206,19 +307,27 @@ cudaError_t launch_direct_f32(const GroupDesc& gd, bool fwd, const void* in, voi
   GroupDesc g = gd;
   set_divisors(g);
   const int C = kDirectPoints / d.M;
-  // the layout the kernel is compiled for: columns in, rows (first group) or columns out
-  const bool ok = g.M == d.M && g.nsub == d.nsub && g.npass == 2 && g.in_sub == 1 &&
-                  g.in_elem == d.nsub && (g.twsub != 0) == (d.twsub != 0) &&
-                  (d.twsub ? (g.out_sub == 1 && g.out_elem == d.nsub)
-                           : (g.out_sub == d.M && g.out_elem == 1)) &&
-                  g.total_sub % C == 0;
+  const int np = d.r[2] > 0 ? 3 : 2;
+  bool ok = g.M == d.M && g.npass == np;
+  for (int t = 0; t < np && ok; ++t) ok = g.pass[t].R == d.r[t];
+  // the layout the kernel is compiled for
+  if (d.layout == kSingle) {
+    ok = ok && g.in_elem == 1 && g.out_elem == 1 && g.in_sub == 0 && g.out_sub == 0 &&
+         g.twsub == 0;
+  } else {
+    ok = ok && g.nsub == d.nsub && g.in_sub == 1 && g.in_elem == d.nsub &&
+         (g.twsub != 0) == (d.layout == kSecondOfTwo) &&
+         (d.layout == kSecondOfTwo ? (g.out_sub == 1 && g.out_elem == d.nsub)
+                                   : (g.out_sub == d.M && g.out_elem == 1)) &&
+         g.total_sub % C == 0;
+  }
   if (!ok) return cudaErrorInvalidValue;
-  const int64_t ntiles = g.total_sub / C;
+  const int64_t ntiles = (g.total_sub + C - 1) / C;
   if (ntiles == 0) return cudaSuccess;
   if (ntiles > 0x7fffffff) return cudaErrorInvalidValue;
   const DirectFn kern = fwd ? direct_fn<true>(variant) : direct_fn<false>(variant);
-  kern<<<(unsigned)ntiles, kDirectThreads, 0, stream>>>(g, static_cast<const float2*>(in),
-                                                        static_cast<float2*>(out));
+  kern<<<(unsigned)ntiles, kDirectThreads, direct_smem(variant), stream>>>(
+      g, static_cast<const float2*>(in), static_cast<float2*>(out));
   return cudaGetLastError();
 }
 

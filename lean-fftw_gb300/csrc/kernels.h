@@ -58,13 +58,16 @@ int tile_variant_f32(const GroupDesc& g);
 cudaError_t launch_tile_stream_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                                    unsigned grid, cudaStream_t stream, int variant = -1);
 
-// Register-staged FP32 kernel for a two-pass group of a two-group plan over contiguous lines
-// (first pass from global memory, last pass to global memory, one shared tile between):
-// direct_variant_f32 gives the compiled variant of a group (M points, the other group's size
-// nsub, second group, compensated twiddles, its radices) or -1.  A second group run by it
-// takes its twiddle tables in pass order (not transposed).  The launch checks the group's
-// strides against the compiled layout and refuses any other.
-int direct_variant_f32(int M, int nsub, bool twsub, bool comp, const int* radices, int npass);
+// Register-staged FP32 kernel for a group of two or three passes over contiguous lines (first
+// pass from global memory, last pass to global memory, shared tiles between): the first or
+// second group of a two-group plan, or the one group of a one-group plan.
+// direct_variant_f32 gives the compiled variant of a group (layout, M points, the other
+// group's size nsub (1 for one group), compensated twiddles, its radices) or -1.  A second
+// group run by it takes its twiddle tables in pass order (not transposed).  The launch checks
+// the group's strides against the compiled layout and refuses any other.
+enum DirectLayoutKind { kDirectFirstOfTwo = 0, kDirectSecondOfTwo = 1, kDirectSingle = 2 };
+int direct_variant_f32(int layout, int M, int nsub, bool comp, const int* radices, int npass);
+cudaError_t prepare_direct_kernels_f32();
 cudaError_t launch_direct_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                               int variant, cudaStream_t stream);
 

@@ -161,7 +161,7 @@ int choose_split(int64_t N, std::vector<int>& rs, int64_t single_max, int prec, 
 // Largest binary32 size run as one pass group by default.  Binary32 is bound by HBM, and a
 // one-group tile above this size leaves one CTA per SM; larger sizes run two groups of about
 // sqrt(n) points each (choose_radices orders the radices for that split).
-constexpr int64_t kF32SingleGroupMax = 8192;
+constexpr int64_t kF32SingleGroupMax = 4096;
 
 // Codelet operation count of a plan's radix sequence, per transform.
 double plan_ops(int64_t n, const std::vector<int>& radices);

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -25,6 +26,13 @@ namespace {
 }  // namespace
 
 bool radix_ok(int R) { return R >= 2 && R <= kMaxRadix && kOpsUntw[R] > 0; }
+
+// LFG_DIRECT=0 in the environment (read at planning): binary32 plans use the copy-staged
+// kernels instead of the register-staged ones (for comparisons; the same bits).
+static bool direct_enabled() {
+  const char* s = std::getenv("LFG_DIRECT");
+  return !(s && s[0] == '0');
+}
 
 namespace {
 
@@ -435,11 +443,12 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   // register-staged kernel: the second group reads its tables in pass order
   p.direct_variant[0] = p.direct_variant[1] = -1;
   if (prec == 1 && split > 0 && split < (int)rs.size() && !p.generic_kernels &&
-      p.howmany2 == 1 && p.in.stride == 1 && p.out.stride == 1) {
+      p.howmany2 == 1 && p.in.stride == 1 && p.out.stride == 1 && direct_enabled()) {
     int64_t P = 1;
     for (int t = 0; t < split; ++t) P *= rs[t];
-    const int v1 = direct_variant_f32((int)P, (int)(N / P), false, false, rs.data(), split);
-    const int v2 = direct_variant_f32((int)(N / P), (int)P, true, comp[split] != 0,
+    const int v1 = direct_variant_f32(kDirectFirstOfTwo, (int)P, (int)(N / P), false, rs.data(),
+                                      split);
+    const int v2 = direct_variant_f32(kDirectSecondOfTwo, (int)(N / P), (int)P, comp[split] != 0,
                                       rs.data() + split, (int)rs.size() - split);
     if (v1 >= 0 && v2 >= 0) {
       p.direct_variant[0] = v1;
@@ -531,6 +540,16 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
       p.stream_grid = (unsigned)std::max<int64_t>(1, std::min(want, tiles));
       p.stream = true;
     }
+  }
+  // binary32 one-group plans of 2^9 .. 2^12 points over contiguous lines: the register-staged
+  // kernel (the bulk-copy kernel stays for the bounded-wait tests, which need its waits)
+  if (prec == 1 && p.ngroups == 1 && p.howmany2 == 1 && p.in.stride == 1 && p.out.stride == 1 &&
+      p.howmany > 0 && !p.generic_kernels && !p.wait_give_up && direct_enabled()) {
+    bool any_comp = false;
+    for (int t = 0; t < g0.npass; ++t) any_comp = any_comp || g0.pass[t].comp;
+    if (!any_comp)
+      p.direct_variant[0] = direct_variant_f32(kDirectSingle, (int)N, 1, false, rs.data(),
+                                               (int)rs.size());
   }
   if (prec == 1 && !p.stream && p.howmany > 0) {
     // three tile buffers per CTA (stage + two work buffers): shrink C to fit
@@ -814,6 +833,8 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     return launch_group_f32(g, p.fwd, a, b, stream);
   };
   if (p.ngroups == 1) {
+    if (p.direct_variant[0] >= 0)
+      return launch_direct_f32(p.groups[0], p.fwd, ib, ob, p.direct_variant[0], stream);
     if (p.cluster && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)
       return launch_cluster_f64(p.groups[0], p.fwd, ib, ob, p.d_twiddles, p.cluster_tw_len,
                                 stream);

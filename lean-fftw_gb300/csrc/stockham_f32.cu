@@ -704,7 +704,7 @@ cudaError_t prepare_group_kernels_f32() {
     if ((e = allow_max_smem(tile_fn<true>(v))) != cudaSuccess) return e;
     if ((e = allow_max_smem(tile_fn<false>(v))) != cudaSuccess) return e;
   }
-  return cudaSuccess;
+  return prepare_direct_kernels_f32();
 }
 
 size_t tile_stream_smem_bytes_f32(const GroupDesc& g, int variant) {

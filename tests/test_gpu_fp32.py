@@ -59,17 +59,27 @@ def test_fp32_inplace_and_unaligned():
 
 
 @pytest.mark.parametrize("sign", [-1, 1])
-@pytest.mark.parametrize("n", [1 << k for k in range(4, 14)])
+@pytest.mark.parametrize("n", [1 << k for k in range(4, 13)])
 def test_power_of_two_variants_equal_generic_passes(n, sign):
-    """One-group power-of-two plans run a persistent kernel whose passes are compiled for the
-    plan (shifts, masks and immediate offsets instead of runtime index arithmetic).  A buffer
-    offset by one complex value (not 16-byte aligned) takes the generic kernel with runtime
-    pass descriptors: both must give the same bits."""
+    """One-group power-of-two plans run a kernel whose passes are compiled for the plan
+    (shifts, masks and immediate offsets instead of runtime index arithmetic): the
+    register-staged kernel for 2^9 .. 2^12 points (any 8-byte aligned buffer), else the
+    persistent bulk-copy kernel, whose buffers offset by one complex value (not 16-byte
+    aligned) take the generic kernel with runtime pass descriptors.  Every route, and the
+    generic kernels (LFG_GENERIC_KERNELS), must give the same bits; a batch that is not a
+    multiple of the tile leaves a partial last tile."""
     B = max(3, min(64, (1 << 16) // n)) + 1
     x = O.uniform_complex((B + 1, n), seed=n + sign).astype(np.complex64)
     plan = lfg.plan_1d(n, sign, B, precision="f32")
+    assert plan.info().direct_groups == (1 if 512 <= n <= 4096 else 0)
     aligned = torch.from_numpy(x[:B].copy()).cuda()
     fast = plan.execute(aligned)
+    generic = lfg.plan_1d(n, sign, B, precision="f32", generic_kernels=True)
+    assert generic.info().direct_groups == 0
+    assert torch.equal(generic.execute(aligned), fast), n
+    inplace = aligned.clone()
+    plan.execute(inplace, inplace)
+    assert torch.equal(inplace, fast), n
     buf = torch.from_numpy(x.reshape(-1)).cuda()
     un_out = torch.empty(B * n + 1, dtype=torch.complex64, device="cuda")[1:]
     plan.execute(buf[1: 1 + B * n], un_out)                     # 8-byte offset: generic
@@ -84,19 +94,19 @@ def test_power_of_two_variants_equal_generic_passes(n, sign):
 
 @pytest.mark.parametrize("comp", [True, False])
 @pytest.mark.parametrize("sign", [-1, 1])
-@pytest.mark.parametrize("n", [1 << k for k in range(14, 19)])
+@pytest.mark.parametrize("n", [1 << k for k in range(13, 19)])
 def test_two_group_variants_equal_generic_kernels(n, sign, comp):
-    """Two-group power-of-two plans run each group on a kernel compiled for its geometry: the
-    register-staged two-pass kernel up to 2^16 (first pass from global memory, last pass to
-    global memory, second-group tables in pass order), the strided-tile kernel with constant
-    strides above; the generic kernels (LFG_GENERIC_KERNELS) must give the same bits,
-    compensated or not, out of place (the intermediate in the output) and in place."""
+    """Two-group power-of-two plans (2^13 .. 2^18) run each group on the register-staged
+    kernel compiled for its geometry (first pass from global memory, last pass to global
+    memory, second-group tables in pass order); the generic kernels (LFG_GENERIC_KERNELS)
+    must give the same bits, compensated or not, out of place (the intermediate in the
+    output) and in place."""
     B = max(2, (1 << 20) // n)
     x = torch.from_numpy(O.uniform_complex((B, n), seed=n + sign).astype(np.complex64)).cuda()
     fast = lfg.plan_1d(n, sign, B, precision="f32", compensated=comp)
     slow = lfg.plan_1d(n, sign, B, precision="f32", compensated=comp, generic_kernels=True)
     assert fast.info().ngroups == 2
-    assert fast.info().direct_groups == (2 if n <= 1 << 16 else 0)
+    assert fast.info().direct_groups == 2
     assert slow.info().direct_groups == 0
     a, b = fast.execute(x), slow.execute(x)
     torch.cuda.synchronize()

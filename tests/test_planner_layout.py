@@ -32,8 +32,10 @@ def test_known_layouts():
     assert _groups(1 << 24, rs, first) == (4096, 4096)
     rs, first = lfg.plan_layout(16384, "f32")                  # balanced binary32 split
     assert _groups(16384, rs, first) == (128, 128)
-    rs, first = lfg.plan_layout(8192, "f32")                   # binary32: one group to 8192
+    rs, first = lfg.plan_layout(4096, "f32")                   # binary32: one group to 4096
     assert first == len(rs)
+    rs, first = lfg.plan_layout(8192, "f32")                   # then two register-staged groups
+    assert _groups(8192, rs, first) == (128, 64)
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32"])

@@ -42,7 +42,7 @@ def _random(shape, dtype, seed):
 
 @pytest.mark.parametrize("n,howmany,precision,groups", [
     (16384, 32, "f64", 2), (65536, 8, "f64", 2), (1024, 16, "f64", 1),
-    (8192, 64, "f32", 1), (16384, 32, "f32", 2), (65536, 16, "f32", 2)])
+    (4096, 64, "f32", 1), (8192, 64, "f32", 2), (16384, 32, "f32", 2), (65536, 16, "f32", 2)])
 def test_static_scratch_matches_regular_entry(n, howmany, precision, groups):
     dtype = torch.complex128 if precision == "f64" else torch.complex64
     plan = lfg.plan_1d(n, -1, howmany, precision=precision)
