@@ -21,7 +21,7 @@
 // kernel of the library (the generated codelets, the same twiddle values and compensated
 // products), so the bits are the same.  A second group's twiddle tables are kept in pass
 // order (index k P + m: the sub-problem index fastest), which neighbouring threads read as
-// contiguous runs.
+// contiguous runs, and a compensated twiddle as one (hi, lo) quadruple (one 16-byte load).
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -128,12 +128,12 @@ __device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, int6
         x[2 * R + 2 * r + 1] = v.y;
       }
     } else if (MODE == 2) {
-      const float2* __restrict__ wh = tw + kg;
-      const float2* __restrict__ wl = wh + (R - 1) * NSG;
+      // (hi re, hi im, lo re, lo im) per twiddle
+      const float4* __restrict__ w4 = reinterpret_cast<const float4*>(tw) + kg;
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        const float2 h = __ldg(wh + (r - 1) * NSG), l = __ldg(wl + (r - 1) * NSG);
-        const float wrh = h.x, wih = h.y, wrl = l.x, wil = l.y;
+        const float4 q4 = __ldg(w4 + (r - 1) * NSG);
+        const float wrh = q4.x, wih = q4.y, wrl = q4.z, wil = q4.w;
         const float a = x[2 * r], bi = x[2 * r + 1];
         const float cr = P::fma(a, wrl, -P::mul(bi, wil));
         const float ci = P::fma(a, wil, P::mul(bi, wrl));

@@ -194,7 +194,10 @@ int64_t max_single_group(int precision);
 // Store each pass table as (re, im) pairs: row pair (2r, 2r+1) of ns values becomes ns
 // pairs, so a butterfly reads each twiddle with one vector load.  Compensated binary32 tables
 // interleave their hi and lo halves separately.  Applied after transpose_second_group.
-void interleave_tables(PassTables& pt, const std::vector<int>& rs, const std::vector<int>& comp);
+// quads: compensated passes as (hi re, hi im, lo re, lo im) per twiddle instead of a pair table
+// of hi values followed by one of lo values.
+void interleave_tables(PassTables& pt, const std::vector<int>& rs, const std::vector<int>& comp,
+                       bool quads = false);
 int split_point(int64_t N, const std::vector<int>& rs, int64_t max_m);
 // Fill the passes and tile size of a group covering passes t0..t1-1; tw_base is the device
 // copy of PassTables::values.

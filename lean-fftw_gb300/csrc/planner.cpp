@@ -260,10 +260,26 @@ void transpose_second_group(PassTables& pt, const std::vector<int>& rs, int spli
   }
 }
 
-void interleave_tables(PassTables& pt, const std::vector<int>& rs, const std::vector<int>& comp) {
+void interleave_tables(PassTables& pt, const std::vector<int>& rs, const std::vector<int>& comp,
+                       bool quads) {
   std::vector<double> pairs;
   for (size_t t = 1; t < rs.size(); ++t) {
     const int64_t ns = pt.ns[t];
+    if (quads && !comp.empty() && comp[t]) {
+      // (hi re, hi im, lo re, lo im) per twiddle: one 16-byte load in binary32
+      double* v = pt.values.data() + pt.offset[t];
+      const size_t len = 2 * (size_t)(rs[t] - 1) * ns;   // one part
+      pairs.assign(v, v + 2 * len);
+      for (int r = 0; r < rs[t] - 1; ++r)
+        for (int64_t k = 0; k < ns; ++k) {
+          double* q = v + 4 * ((size_t)r * ns + k);
+          q[0] = pairs[(size_t)(2 * r) * ns + k];
+          q[1] = pairs[(size_t)(2 * r + 1) * ns + k];
+          q[2] = pairs[len + (size_t)(2 * r) * ns + k];
+          q[3] = pairs[len + (size_t)(2 * r + 1) * ns + k];
+        }
+      continue;
+    }
     const int parts = !comp.empty() && comp[t] ? 2 : 1;   // hi table, then lo table
     for (int part = 0; part < parts; ++part) {
       double* v = pt.values.data() + pt.offset[t] + (size_t)part * 2 * (rs[t] - 1) * ns;
@@ -456,7 +472,8 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
     }
   }
   if (p.direct_variant[1] < 0) transpose_second_group(pt, rs, split, comp);
-  interleave_tables(pt, rs, comp);
+  // the register-staged kernels read a compensated twiddle as one (hi, lo) quadruple
+  interleave_tables(pt, rs, comp, p.direct_variant[1] >= 0);
   p.d_twiddles = upload_tables(pt.values, prec, &msg);
   if (!p.d_twiddles) return msg;
 
