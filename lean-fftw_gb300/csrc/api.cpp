@@ -1130,7 +1130,7 @@ static lfg_status lfg_get_plan_info_impl(const lfg_plan* plan, lfg_plan_info* in
   info->in_bytes = p.in_span * (p.precision == 0 ? 8 : 4);
   info->out_bytes = p.out_span * (p.precision == 0 ? 8 : 4);
   info->flops = p.flops;
-  info->cluster_ctas = p.cluster ? lfg::cluster_size_f64(p.groups[0]) : 0;
+  info->cluster_ctas = p.cluster ? p.cluster_args.S : 0;
   info->direct_groups = (p.direct_variant[0] >= 0) + (p.direct_variant[1] >= 0);
   return LFG_OK;
 }

@@ -39,14 +39,28 @@ cudaError_t launch_stream_f32(const GroupDesc& g, bool fwd, const void* in, void
 // size n with radices rs, or -1.
 int stream_variant_f32(int64_t n, const std::vector<int>& rs);
 
-// One binary64 transform of N <= kClusterMaxN points (one group, contiguous line) spread over a
-// thread-block cluster of cluster_size_f64(g) CTAs (the latency path of a lone transform);
-// tw_base / tw_len: the plan's whole twiddle table (interleaved pairs), copied into each CTA.
+// One binary64 transform of N <= kClusterMaxN points (one group, contiguous line) on a
+// thread-block cluster (the latency path of a lone transform): the lane groups evaluate each
+// butterfly level by level of its operation DAG.  build_cluster_image_f64 builds, when the
+// plan is made, the device image the kernel copies into shared memory (each pass's geometry,
+// its lane-parallel schedule and its twiddle table, from the plan's interleaved tables
+// tw_values with per-pass offsets tw_offset in doubles) and fills the launch arguments
+// except `img` (the uploaded image), `scale` and `unit` (set at launch); it returns the
+// image's bytes, 0 if the group has no cluster form.
 constexpr int kClusterMaxN = 4096;
+struct ClusterArgs {
+  const void* img;
+  int img_bytes, N, npass, vwarp, R0, W0, nin0, S;
+  double scale;
+  int unit;
+};
 int cluster_size_f64(const GroupDesc& g);
-size_t cluster_smem_bytes_f64(const GroupDesc& g, int tw_len);
-cudaError_t launch_cluster_f64(const GroupDesc& g, bool fwd, const void* in, void* out,
-                               const void* tw_base, int tw_len, cudaStream_t stream);
+size_t build_cluster_image_f64(const GroupDesc& g, bool fwd, const double* tw_values,
+                               const size_t* tw_offset, std::vector<unsigned char>& img,
+                               ClusterArgs* args);
+size_t cluster_smem_bytes_f64(const ClusterArgs& a);
+cudaError_t launch_cluster_f64(const ClusterArgs& a, double scale, const void* in, void* out,
+                               cudaStream_t stream);
 
 // Persistent FP32 kernel for tiles of strided sub-problems (three tile buffers: a stage
 // filled by asynchronous element copies, two work buffers); in and out 8-byte aligned.

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "chirp.h"
+#include "kernels.h"
 #include "generic.h"
 #include "pack.h"
 #include "r2r.h"
@@ -87,7 +88,8 @@ struct Plan {
   int stream_variant = -1;      // compile-time power-of-two variant of that kernel (-1: none)
   // a lone binary64 transform of at most kClusterMaxN points runs on a thread-block cluster
   bool cluster = false;
-  int cluster_tw_len = 0;       // complex entries of the plan's twiddle table
+  ClusterArgs cluster_args{};   // its launch arguments (cluster_f64.cu)
+  void* d_cluster_img = nullptr;   // its device image
   // binary32 groups not covered by the stream kernel: the persistent strided-tile kernel
   // (asynchronous copies of the next tile), one grid per group
   bool tile_stream = false;

@@ -15,6 +15,7 @@
 #include <map>
 
 #include "generated/opcounts.h"
+#include "generated/wide_f64.h"
 #include "kernels.h"
 #include "plan.h"
 #include "real.h"
@@ -127,14 +128,19 @@ std::vector<int> choose_radices(int64_t n, int precision) {
 }
 
 std::vector<int> choose_radices_latency(int64_t n) {
-  // a pass of a lone transform costs the serial binary64 operations of one butterfly (each
-  // warp instruction holds its sub-partition's FP64 pipe for 64 cycles, so butterflies on
-  // other warps are free) times the butterflies per thread (1024 threads at most), plus the
-  // pass's fixed cost -- loads, distributed stores, the cluster barrier -- of kPassFixed
-  // operations' time
-  constexpr double kPassFixed = 12.0;
-  constexpr int64_t kThreads = 1024;
+  // a lone transform runs on a thread-block cluster whose lane groups evaluate each butterfly
+  // level by level of its operation DAG (cluster_f64.cu): a pass costs its schedule's depth
+  // times the rounds its butterflies need on the cluster's 2048 lanes (sixteen CTAs of 128
+  // threads), plus a fixed cost per pass -- input loads, distributed stores, the cluster
+  // barrier -- of kPassFixed levels
+  constexpr double kPassFixed = 5.0;
+  constexpr int64_t kLanes = 2048;
   if (n < 2) return {};
+  auto pass_cost = [&](int R, bool tw) {
+    const WideInfo& w = kWideInfo[1][R][tw ? 1 : 0];
+    const int64_t rounds = ((n / R) * w.W + kLanes - 1) / kLanes;
+    return (double)(rounds * w.depth) + kPassFixed;
+  };
   std::map<int64_t, std::pair<double, std::vector<int>>> memo;   // twiddled tail of length m
   std::function<const std::pair<double, std::vector<int>>&(int64_t)> tail =
       [&](int64_t m) -> const std::pair<double, std::vector<int>>& {
@@ -146,8 +152,7 @@ std::vector<int> choose_radices_latency(int64_t n) {
         if (!radix_ok(R) || m % R) continue;
         const auto& t = tail(m / R);
         if (!std::isfinite(t.first)) continue;
-        const double per = (double)((n / R + kThreads - 1) / kThreads);
-        const double c = kOpsTw[R] * per + kPassFixed + t.first;
+        const double c = pass_cost(R, true) + t.first;
         if (c < best.first - 1e-12) {
           best.first = c;
           best.second = t.second;
@@ -162,8 +167,7 @@ std::vector<int> choose_radices_latency(int64_t n) {
     if (!radix_ok(R0) || n % R0) continue;
     const auto& t = tail(n / R0);
     if (!std::isfinite(t.first)) continue;
-    const double per = (double)((n / R0 + kThreads - 1) / kThreads);
-    const double c = kOpsUntw[R0] * per + kPassFixed + t.first;
+    const double c = pass_cost(R0, false) + t.first;
     if (c < best - 1e-12) {
       best = c;
       seq = t.second;
@@ -194,6 +198,9 @@ void free_plan_memory(Plan& p) {
   if (p.d_r2r_buf) cudaFree(p.d_r2r_buf);
   if (p.d_gen_tab) cudaFree(p.d_gen_tab);
   p.d_gen_tab = nullptr;
+  if (p.d_cluster_img) cudaFree(p.d_cluster_img);
+  p.d_cluster_img = nullptr;
+  p.cluster = false;
   if (p.d_pack_buf) cudaFree(p.d_pack_buf);
   p.d_pack_buf = nullptr;
   for (PackStep& st : p.steps)
@@ -533,10 +540,24 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
       p.groups[gi].pass[t].comp = comp[p.group_first_pass[gi] + t];
   // a lone binary64 transform of a contiguous line: the thread-block cluster kernel
   p.cluster = false;
+  if (p.d_cluster_img) cudaFree(p.d_cluster_img);
+  p.d_cluster_img = nullptr;
   if (prec == 0 && p.ngroups == 1 && p.howmany == 1 && p.howmany2 == 1 && p.stages.empty() &&
       p.in.stride == 1 && p.out.stride == 1 && cluster_size_f64(p.groups[0]) > 0) {
-    p.cluster_tw_len = (int)(pt.values.size() / 2);
-    p.cluster = cluster_smem_bytes_f64(p.groups[0], p.cluster_tw_len) <= kSmemBudget;
+    std::vector<unsigned char> img;
+    ClusterArgs ca{};
+    if (build_cluster_image_f64(p.groups[0], p.fwd, pt.values.data(), pt.offset.data(), img, &ca) > 0 &&
+        cluster_smem_bytes_f64(ca) <= kSmemBudget &&
+        cudaMalloc(&p.d_cluster_img, img.size()) == cudaSuccess) {
+      if (cudaMemcpy(p.d_cluster_img, img.data(), img.size(), cudaMemcpyHostToDevice) == cudaSuccess) {
+        ca.img = p.d_cluster_img;
+        p.cluster_args = ca;
+        p.cluster = true;
+      } else {
+        cudaFree(p.d_cluster_img);
+        p.d_cluster_img = nullptr;
+      }
+    }
   }
   // binary32 over back-to-back lines: the persistent kernel with bulk-copy prefetch
   const GroupDesc& g0 = p.groups[0];
@@ -853,8 +874,7 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
     if (p.direct_variant[0] >= 0)
       return launch_direct_f32(p.groups[0], p.fwd, ib, ob, p.direct_variant[0], stream);
     if (p.cluster && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)
-      return launch_cluster_f64(p.groups[0], p.fwd, ib, ob, p.d_twiddles, p.cluster_tw_len,
-                                stream);
+      return launch_cluster_f64(p.cluster_args, p.groups[0].scale, ib, ob, stream);
     // the bulk-copy engine needs 16-byte aligned ranges; in place is fine (each tile is read
     // into shared memory before it is written)
     if (p.stream && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)

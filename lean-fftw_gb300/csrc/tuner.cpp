@@ -286,6 +286,7 @@ std::string tune_c2c(Plan& p, int64_t default_tile) {
         c.radices = rs;
         c.single_max = sm;
         c.d_twiddles = c.d_scratch = c.d_host_in = c.d_host_out = nullptr;
+        c.d_cluster_img = nullptr;
         std::string msg = build_c2c(c, tile);
         if (!msg.empty()) {
           free_plan_memory(c);

@@ -4,8 +4,9 @@
 
 1. Runs the restated lean-fftw codelet generator (lfg.codegen) and writes
    csrc/generated/codelets_f64.cuh (device butterflies, one template specialisation per
-   radix, direction and twiddling) and csrc/generated/opcounts.h (operation counts used by
-   the planner).
+   radix, direction and twiddling), csrc/generated/opcounts.h (operation counts used by
+   the planner) and csrc/generated/wide_f64.h (lane-parallel schedules of the
+   binary64 butterflies for the lone-transform cluster kernel).
 2. Compiles csrc/*.cu for sm_103a (nvcc -gencode arch=compute_103a,code=sm_103a) and the
    host sources with g++, in parallel, and links lfg/liblfg.so.
 3. Builds the libbench2-style command line lfg/lfg-bench (csrc/tools/lfg_bench.cpp) against
@@ -73,6 +74,8 @@ def generate() -> None:
             f"constexpr int kOpsTw[17] = {{{', '.join(map(str, tw))}}};\n"
             "}  // namespace lfg\n")
     _write_if_changed(os.path.join(GEN, "opcounts.h"), text)
+    from lfg.codegen.wide import c_tables
+    _write_if_changed(os.path.join(GEN, "wide_f64.h"), c_tables(GPU_RADICES))
 
 
 def _sources():
