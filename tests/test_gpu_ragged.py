@@ -123,6 +123,28 @@ def test_ragged_pinned_host_entry():
     assert not _check(plan, sizes, x, hout.numpy(), plan.in_offsets, plan.out_offsets)
 
 
+def test_ragged_host_pageable_and_gapped():
+    """Pageable host arrays (copied in and out around the launch); and pinned buffers whose
+    inputs and outputs leave gaps (the kernel reads and writes host memory directly): the
+    caller's values in the output gaps stay."""
+    sizes = lfg.ragged_sizes(256, seed=8)
+    plan = lfg.plan_ragged(sizes, -1)
+    x = O.uniform_complex((int(sizes.sum()),), seed=9)
+    y = plan.execute_host(x, np.zeros_like(x))
+    assert not _check(plan, sizes, x, y, plan.in_offsets, plan.out_offsets)
+    in_off = np.concatenate([[0], np.cumsum(sizes + 5)[:-1]]).astype(np.int64)
+    out_off = np.concatenate([[0], np.cumsum(sizes + 3)[:-1]]).astype(np.int64)
+    gapped = lfg.plan_ragged(sizes, -1, in_offsets=in_off, out_offsets=out_off)
+    xg = O.uniform_complex((int(in_off[-1] + sizes[-1]),), seed=10)
+    hin = torch.from_numpy(xg).pin_memory()
+    hout = torch.full((int(out_off[-1] + sizes[-1]),), SENT, dtype=torch.complex128).pin_memory()
+    gapped.execute_host(hin.numpy(), hout.numpy())
+    y2 = hout.numpy()
+    assert not _check(gapped, sizes, xg, y2, in_off, out_off)
+    for o, n in zip(out_off, sizes):
+        assert np.all(y2[o + n: o + n + 3] == SENT)     # (empty past the last output)
+
+
 @pytest.mark.parametrize("shape", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("tile,single", [(2048, 2048), (4096, 4096), (1024, 1024)])
 def test_ragged_block_shapes(shape, tile, single):
