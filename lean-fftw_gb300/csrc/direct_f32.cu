@@ -31,8 +31,7 @@ namespace lfg {
 using namespace dev;
 namespace {
 
-constexpr int kDirectThreads = 256;
-constexpr int kDirectPoints = 4096;   // points per tile
+constexpr int kDirectPoints = 4096;   // points per tile (16 per thread)
 
 // Global layouts of a group's sub-problems (element i of sub-problem c of the tile):
 //   kFirstOfTwo   in c + i NSUB (columns), out c M + i (rows)
@@ -47,6 +46,13 @@ enum DirectDst { kToTile = 0, kToRows = 1, kToCols = 2 };
 // Tile pitch: odd for tiles of 16 or more sub-problems, 2 mod 16 for 8 (a half-warp then
 // spans 8 sub-problems and two neighbouring elements), the padded length otherwise (those
 // passes walk along the sub-problem).
+// Sub-problems per tile and threads per CTA: 4096-point tiles, except the 512-point groups of
+// two-group plans, whose tiles of 16 columns (128-byte runs) hold 8192 points on 512 threads.
+LFG_HD constexpr int direct_width(int layout, int M) {
+  return layout != kDirectSingle && M == 512 ? 16 : kDirectPoints / M;
+}
+LFG_HD constexpr int direct_threads(int layout, int M) { return direct_width(layout, M) * M / 16; }
+
 LFG_HD constexpr int direct_pitch(int M, int C) {
   return C >= 16 ? (sub_pitch(M) | 1) : (C == 8 ? sub_pitch(M) + ((2 - sub_pitch(M)) & 15) : sub_pitch(M));
 }
@@ -57,8 +63,8 @@ LFG_HD constexpr int direct_pitch(int M, int C) {
 // 2 compensated (hi, lo) twiddles.  `gin` / `gout`: the tile's first element in global
 // memory; ldi / ldo: line distances of rows; count: sub-problems of the tile present (rows
 // only; the others are never loaded or stored).
-template <bool FWD, int M, int C, int PM, int R, int NSL, int NSUB, bool TWSUB, int MODE, int SRC,
-          int DST>
+template <bool FWD, int M, int C, int PM, int T, int R, int NSL, int NSUB, bool TWSUB, int MODE,
+          int SRC, int DST>
 __device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, int64_t ldi,
                                             const float2* src, float2* dst,
                                             float2* __restrict__ gout, int64_t ldo,
@@ -73,11 +79,11 @@ __device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, int6
   // (its twiddles are contiguous across sub-problems), along them where a row is
   constexpr bool CFAST = (SRC == kFromCols || DST == kToCols || TWSUB) && SRC != kFromRows &&
                          DST != kToRows;
-  static_assert(NB % kDirectThreads == 0, "whole butterflies per thread");
+  static_assert(NB % T == 0, "whole butterflies per thread");
   const float one = 1.0f, nz = -0.0f;   // (the binary32 codelets do not use them)
 #pragma unroll
-  for (int it = 0; it < NB / kDirectThreads; ++it) {
-    const int q = (int)threadIdx.x + it * kDirectThreads;
+  for (int it = 0; it < NB / T; ++it) {
+    const int q = (int)threadIdx.x + it * T;
     const int c = CFAST ? q % C : q / MR;
     const int j = CFAST ? q / C : q % MR;
     float x[TW ? 4 * R - 2 : 2 * R];
@@ -167,10 +173,11 @@ __device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, int6
 // A group of two or three passes (radices R0, R1, R2; R2 = 0: two) of M points; NSUB = the
 // other group's size (two-group layouts).
 template <bool FWD, int LAYOUT, int M, int NSUB, bool COMP, int R0, int R1, int R2>
-__global__ void __launch_bounds__(kDirectThreads, 3)
+__global__ void __launch_bounds__(direct_threads(LAYOUT, M), direct_threads(LAYOUT, M) > 256 ? 1 : 3)
 direct_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
   constexpr bool TWSUB = LAYOUT == kSecondOfTwo;
-  constexpr int C = kDirectPoints / M;
+  constexpr int C = direct_width(LAYOUT, M);
+  constexpr int T = direct_threads(LAYOUT, M);
   constexpr int PM = direct_pitch(M, C);
   constexpr int MODE_T = TWSUB ? (COMP ? 2 : 1) : 1;
   constexpr int SRC0 = LAYOUT == kSingle ? kFromRows : kFromCols;
@@ -200,18 +207,18 @@ direct_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
   const float sc = g.scale_f32;
   const float2* tw0 = static_cast<const float2*>(g.pass[0].tw);
   const float2* tw1 = static_cast<const float2*>(g.pass[1].tw);
-  direct_pass<FWD, M, C, PM, R0, 1, NSUB, TWSUB, TWSUB ? MODE_T : 0, SRC0, kToTile>(
+  direct_pass<FWD, M, C, PM, T, R0, 1, NSUB, TWSUB, TWSUB ? MODE_T : 0, SRC0, kToTile>(
       gin, ldi, nullptr, A, nullptr, 0, tw0, sub0, count, true, 1.0f);
   __syncthreads();
   if constexpr (R2 > 0) {
-    direct_pass<FWD, M, C, PM, R1, R0, NSUB, TWSUB, MODE_T, kFromTile, kToTile>(
+    direct_pass<FWD, M, C, PM, T, R1, R0, NSUB, TWSUB, MODE_T, kFromTile, kToTile>(
         nullptr, 0, A, B, nullptr, 0, tw1, sub0, count, true, 1.0f);
     __syncthreads();
-    direct_pass<FWD, M, C, PM, R2, R0 * R1, NSUB, TWSUB, MODE_T, kFromTile, DSTL>(
+    direct_pass<FWD, M, C, PM, T, R2, R0 * R1, NSUB, TWSUB, MODE_T, kFromTile, DSTL>(
         nullptr, 0, B, nullptr, gout, ldo, static_cast<const float2*>(g.pass[2].tw), sub0,
         count, unit, sc);
   } else {
-    direct_pass<FWD, M, C, PM, R1, R0, NSUB, TWSUB, MODE_T, kFromTile, DSTL>(
+    direct_pass<FWD, M, C, PM, T, R1, R0, NSUB, TWSUB, MODE_T, kFromTile, DSTL>(
         nullptr, 0, A, nullptr, gout, ldo, tw1, sub0, count, unit, sc);
   }
 }
@@ -267,7 +274,7 @@ DirectFn direct_fn(int v) {
 
 size_t direct_smem(int v) {
   const DirectGroup& d = kDirectGroups[v];
-  const int C = kDirectPoints / d.M;
+  const int C = direct_width(d.layout, d.M);
   const int tiles = d.r[2] > 0 ? 2 : 1;
   return (size_t)tiles * C * direct_pitch(d.M, C) * sizeof(float2);
 }
@@ -306,7 +313,7 @@ cudaError_t launch_direct_f32(const GroupDesc& gd, bool fwd, const void* in, voi
   const DirectGroup& d = kDirectGroups[variant];
   GroupDesc g = gd;
   set_divisors(g);
-  const int C = kDirectPoints / d.M;
+  const int C = direct_width(d.layout, d.M);
   const int np = d.r[2] > 0 ? 3 : 2;
   bool ok = g.M == d.M && g.npass == np;
   for (int t = 0; t < np && ok; ++t) ok = g.pass[t].R == d.r[t];
@@ -326,7 +333,7 @@ cudaError_t launch_direct_f32(const GroupDesc& gd, bool fwd, const void* in, voi
   if (ntiles == 0) return cudaSuccess;
   if (ntiles > 0x7fffffff) return cudaErrorInvalidValue;
   const DirectFn kern = fwd ? direct_fn<true>(variant) : direct_fn<false>(variant);
-  kern<<<(unsigned)ntiles, kDirectThreads, direct_smem(variant), stream>>>(
+  kern<<<(unsigned)ntiles, direct_threads(d.layout, d.M), direct_smem(variant), stream>>>(
       g, static_cast<const float2*>(in), static_cast<float2*>(out));
   return cudaGetLastError();
 }
