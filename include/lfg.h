@@ -49,7 +49,8 @@ typedef enum { LFG_F64 = 0, LFG_F32 = 1 } lfg_precision;
  * such a plan computes nothing useful; lfg_device_status then returns LFG_ERR_TIMEOUT. */
 #define LFG_TEST_WAIT_GIVE_UP 32u
 /* Run the kernels with runtime pass descriptors even where a kernel compiled for the plan's
- * geometry exists (binary32 power-of-two plans): the same bits, for comparing the two. */
+ * geometry exists (binary32 power-of-two complex plans, and the rows and columns of binary32
+ * real plans): the same bits, for comparing the two. */
 #define LFG_GENERIC_KERNELS 128u
 
 typedef struct lfg_plan lfg_plan;

@@ -394,6 +394,7 @@ lfg_status plan_real_common(bool r2c, size_t n0, size_t n, size_t howmany, lfg_p
   L.c_bdist = (int64_t)(n0 * (n / 2 + 1));
   if ((flags & LFG_ADJOINT) && n0 > 1) return fail(LFG_ERR_UNSUPPORTED, "adjoint scaling is 1-D only");
   p.real.adjoint = (flags & LFG_ADJOINT) ? 1 : 0;
+  p.generic_kernels = (flags & LFG_GENERIC_KERNELS) != 0;
   return finish_real(p, L, out);
 }
 

@@ -24,151 +24,13 @@
 // contiguous runs, and a compensated twiddle as one (hi, lo) quadruple (one 16-byte load).
 #include <cuda_runtime.h>
 
+#include "direct_dev.cuh"
 #include "kernels.h"
-#include "stockham_dev.cuh"
 
 namespace lfg {
 using namespace dev;
 namespace {
-
-constexpr int kDirectPoints = 4096;   // points per tile (16 per thread)
-
-// Global layouts of a group's sub-problems (element i of sub-problem c of the tile):
-//   kFirstOfTwo   in c + i NSUB (columns), out c M + i (rows)
-//   kSecondOfTwo  in columns, out c + i NSUB (columns)
-//   kSingle       in c LDI + i, out c LDO + i (rows at the plan's line distances)
-constexpr int kFirstOfTwo = kDirectFirstOfTwo;
-constexpr int kSecondOfTwo = kDirectSecondOfTwo;
-constexpr int kSingle = kDirectSingle;
-enum DirectSrc { kFromTile = 0, kFromCols = 1, kFromRows = 2 };
-enum DirectDst { kToTile = 0, kToRows = 1, kToCols = 2 };
-
-// Tile pitch: odd for tiles of 16 or more sub-problems, 2 mod 16 for 8 (a half-warp then
-// spans 8 sub-problems and two neighbouring elements), the padded length otherwise (those
-// passes walk along the sub-problem).
-// Sub-problems per tile and threads per CTA: 4096-point tiles, except the 512-point groups of
-// two-group plans, whose tiles of 16 columns (128-byte runs) hold 8192 points on 512 threads.
-LFG_HD constexpr int direct_width(int layout, int M) {
-  return layout != kDirectSingle && M == 512 ? 16 : kDirectPoints / M;
-}
-LFG_HD constexpr int direct_threads(int layout, int M) { return direct_width(layout, M) * M / 16; }
-
-LFG_HD constexpr int direct_pitch(int M, int C) {
-  return C >= 16 ? (sub_pitch(M) | 1) : (C == 8 ? sub_pitch(M) + ((2 - sub_pitch(M)) & 15) : sub_pitch(M));
-}
-
-// One pass with compile-time geometry: sub-problems of M points, tile of C sub-problems at
-// pitch PM, radix R, NSL = product of the group's earlier radices, NSUB = the other group's
-// size; TWSUB: a second group (twiddle index k * NSUB + m); MODE 0 untwiddled, 1 twiddled,
-// 2 compensated (hi, lo) twiddles.  `gin` / `gout`: the tile's first element in global
-// memory; ldi / ldo: line distances of rows; count: sub-problems of the tile present (rows
-// only; the others are never loaded or stored).
-template <bool FWD, int M, int C, int PM, int T, int R, int NSL, int NSUB, bool TWSUB, int MODE,
-          int SRC, int DST>
-__device__ __forceinline__ void direct_pass(const float2* __restrict__ gin, int64_t ldi,
-                                            const float2* src, float2* dst,
-                                            float2* __restrict__ gout, int64_t ldo,
-                                            const float2* __restrict__ tw, int sub0, int count,
-                                            bool unit, float sc) {
-  using P = Prec<float>;
-  constexpr int MR = M / R;
-  constexpr int NB = C * MR;
-  constexpr int NSG = TWSUB ? NSUB * NSL : NSL;
-  constexpr bool TW = MODE == 1;
-  // across sub-problems where a column is read or written and for a second group's passes
-  // (its twiddles are contiguous across sub-problems), along them where a row is
-  constexpr bool CFAST = (SRC == kFromCols || DST == kToCols || TWSUB) && SRC != kFromRows &&
-                         DST != kToRows;
-  static_assert(NB % T == 0, "whole butterflies per thread");
-  const float one = 1.0f, nz = -0.0f;   // (the binary32 codelets do not use them)
-#pragma unroll
-  for (int it = 0; it < NB / T; ++it) {
-    const int q = (int)threadIdx.x + it * T;
-    const int c = CFAST ? q % C : q / MR;
-    const int j = CFAST ? q / C : q % MR;
-    float x[TW ? 4 * R - 2 : 2 * R];
-    float y[2 * R];
-    if (SRC == kFromCols) {
-      const float2* s = gin + c + j * NSUB;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float2 v = s[r * MR * NSUB];
-        x[2 * r] = v.x;
-        x[2 * r + 1] = v.y;
-      }
-    } else if (SRC == kFromRows) {
-      const float2* s = gin + c * ldi + j;
-      const bool present = c < count;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float2 v = present ? s[r * MR] : make_float2(0.0f, 0.0f);
-        x[2 * r] = v.x;
-        x[2 * r + 1] = v.y;
-      }
-    } else if (MR % 16 == 0) {
-      const float2* s = src + c * PM + spad(j);
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float2 v = s[r * (MR + MR / 16)];
-        x[2 * r] = v.x;
-        x[2 * r + 1] = v.y;
-      }
-    } else {
-      const float2* s = src + c * PM;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float2 v = s[spad(j + r * MR)];
-        x[2 * r] = v.x;
-        x[2 * r + 1] = v.y;
-      }
-    }
-    const int b = j / NSL;
-    const int k = j % NSL;
-    const int kg = TWSUB ? k * NSUB + sub0 + c : k;
-    if (MODE == 1) {
-      const float2* __restrict__ w = tw + kg;
-#pragma unroll
-      for (int r = 0; r < R - 1; ++r) {
-        const float2 v = __ldg(w + r * NSG);
-        x[2 * R + 2 * r] = v.x;
-        x[2 * R + 2 * r + 1] = v.y;
-      }
-    } else if (MODE == 2) {
-      // (hi re, hi im, lo re, lo im) per twiddle
-      const float4* __restrict__ w4 = reinterpret_cast<const float4*>(tw) + kg;
-#pragma unroll
-      for (int r = 1; r < R; ++r) {
-        const float4 q4 = __ldg(w4 + (r - 1) * NSG);
-        const float wrh = q4.x, wih = q4.y, wrl = q4.z, wil = q4.w;
-        const float a = x[2 * r], bi = x[2 * r + 1];
-        const float cr = P::fma(a, wrl, -P::mul(bi, wil));
-        const float ci = P::fma(a, wil, P::mul(bi, wrl));
-        x[2 * r] = P::fma(a, wrh, P::fma(-bi, wih, cr));
-        x[2 * r + 1] = P::fma(a, wih, P::fma(bi, wrh, ci));
-      }
-    }
-    BflyF<FWD, R, TW>::run(x, y, one, nz);
-    const int d0 = b * NSL * R + k;
-    if (DST == kToTile) {
-      float2* o = dst + c * PM;
-      if (NSL % 16 == 0) {
-#pragma unroll
-        for (int r = 0; r < R; ++r) o[spad(d0) + r * (NSL + NSL / 16)] = make_float2(y[2 * r], y[2 * r + 1]);
-      } else {
-#pragma unroll
-        for (int r = 0; r < R; ++r) o[spad(d0 + r * NSL)] = make_float2(y[2 * r], y[2 * r + 1]);
-      }
-    } else if (DST == kToCols || c < count) {
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const float2 v = unit ? make_float2(y[2 * r], y[2 * r + 1])
-                              : make_float2(__fmul_rn(y[2 * r], sc), __fmul_rn(y[2 * r + 1], sc));
-        if (DST == kToRows) gout[c * ldo + d0 + r * NSL] = v;
-        else gout[c + (d0 + r * NSL) * NSUB] = v;
-      }
-    }
-  }
-}
+using namespace dfx;
 
 // A group of two or three passes (radices R0, R1, R2; R2 = 0: two) of M points; NSUB = the
 // other group's size (two-group layouts).
@@ -223,6 +85,72 @@ direct_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
   }
 }
 
+using DirectFn = void (*)(const GroupDesc, const float2*, float2*);
+
+// The columns of a batch of images (the first axis of a rank-2 plan): sub-problem s is column
+// s mod nsub of image s / nsub, element i at line * line_dist + col * sub_stride + i * elem
+// (input and output alike, their own strides).  A CTA of M threads takes 16 neighbouring
+// sub-problems (a tile may straddle two images); each thread's column base is computed once,
+// the first pass loads across the 16 columns (128-byte runs), the last pass stores likewise.
+template <bool FWD, int M, int R0, int R1, int R2>
+__global__ void __launch_bounds__(M, M > 256 ? 1 : 2)
+direct_cols_kernel_f32(const GroupDesc g, const float2* in, float2* out) {
+  constexpr int C = 16;
+  constexpr int T = M;
+  constexpr int PM = direct_pitch(M, C);
+  static_assert(M == R0 * R1 * (R2 > 0 ? R2 : 1), "tile geometry");
+  extern __shared__ float2 smem_direct[];
+  float2* A = smem_direct;
+  float2* B = smem_direct + C * PM;
+  const int c = (int)threadIdx.x % C;   // the thread's column in the first and last passes
+  const int64_t sidx = (int64_t)blockIdx.x * C + c;
+  const bool valid = sidx < g.total_sub;
+  const int64_t line = valid ? sidx / g.nsub : 0;
+  const int64_t col = valid ? sidx - line * g.nsub : 0;
+  const float2* tin = in + line * g.in_line + col * g.in_sub;
+  float2* tout = out + line * g.out_line + col * g.out_sub;
+  const bool unit = g.unit_scale != 0;
+  const float sc = g.scale_f32;
+  const float2* tw1 = static_cast<const float2*>(g.pass[1].tw);
+  direct_pass<FWD, M, C, PM, T, R0, 1, 0, false, 0, kFromColsRT, kToTile>(
+      nullptr, 0, nullptr, A, nullptr, 0, nullptr, 0, C, true, 1.0f, tin, nullptr, g.in_elem, valid);
+  __syncthreads();
+  if constexpr (R2 > 0) {
+    direct_pass<FWD, M, C, PM, T, R1, R0, 0, false, 1, kFromTile, kToTile>(
+        nullptr, 0, A, B, nullptr, 0, tw1, 0, C, true, 1.0f);
+    __syncthreads();
+    direct_pass<FWD, M, C, PM, T, R2, R0 * R1, 0, false, 1, kFromTile, kToColsRT>(
+        nullptr, 0, B, nullptr, nullptr, 0, static_cast<const float2*>(g.pass[2].tw), 0, C, unit,
+        sc, nullptr, tout, g.out_elem, valid);
+  } else {
+    direct_pass<FWD, M, C, PM, T, R1, R0, 0, false, 1, kFromTile, kToColsRT>(
+        nullptr, 0, A, nullptr, nullptr, 0, tw1, 0, C, unit, sc, nullptr, tout, g.out_elem, valid);
+  }
+}
+
+struct DirectCols {
+  int M, r[3];
+};
+constexpr DirectCols kDirectCols[] = {
+    {64, {16, 4, 0}}, {128, {16, 8, 0}}, {256, {16, 16, 0}}, {512, {16, 16, 2}}};
+constexpr int kDirectColVariants = (int)(sizeof(kDirectCols) / sizeof(kDirectCols[0]));
+
+template <bool FWD>
+DirectFn direct_cols_fn(int v) {
+  switch (v) {
+    case 0: return direct_cols_kernel_f32<FWD, 64, 16, 4, 0>;
+    case 1: return direct_cols_kernel_f32<FWD, 128, 16, 8, 0>;
+    case 2: return direct_cols_kernel_f32<FWD, 256, 16, 16, 0>;
+    case 3: return direct_cols_kernel_f32<FWD, 512, 16, 16, 2>;
+    default: return nullptr;
+  }
+}
+
+size_t direct_cols_smem(int v) {
+  const DirectCols& d = kDirectCols[v];
+  return (size_t)(d.r[2] > 0 ? 2 : 1) * 16 * direct_pitch(d.M, 16) * sizeof(float2);
+}
+
 // The groups with a kernel here: layout, M, the other group's size (1 for one group),
 // compensated twiddles, radices.  They are the groups of the planner's binary32 plans of
 // 2^9 .. 2^12 (one group) and 2^13 .. 2^18 (two groups: 16.8 | 16.4, 16.8 | 16.8,
@@ -243,8 +171,6 @@ constexpr DirectGroup kDirectGroups[] = {
     {kSingle, 4096, 1, 0, {16, 16, 16}},        {kFirstOfTwo, 128, 64, 0, {16, 8, 0}},
     {kSecondOfTwo, 64, 128, 0, {16, 4, 0}}};
 constexpr int kDirectVariants = (int)(sizeof(kDirectGroups) / sizeof(kDirectGroups[0]));
-
-using DirectFn = void (*)(const GroupDesc, const float2*, float2*);
 
 template <bool FWD>
 DirectFn direct_fn(int v) {
@@ -294,7 +220,47 @@ int direct_variant_f32(int layout, int M, int nsub, bool comp, const int* radice
   return -1;
 }
 
+int direct_cols_variant_f32(int M, const int* radices, int npass) {
+  if (npass != 2 && npass != 3) return -1;
+  for (int v = 0; v < kDirectColVariants; ++v) {
+    const DirectCols& d = kDirectCols[v];
+    if (d.M != M || (d.r[2] > 0 ? 3 : 2) != npass) continue;
+    bool same = true;
+    for (int t = 0; t < npass; ++t) same = same && d.r[t] == radices[t];
+    if (same) return v;
+  }
+  return -1;
+}
+
+cudaError_t launch_direct_cols_f32(const GroupDesc& gd, bool fwd, const void* in, void* out,
+                                   int variant, cudaStream_t stream) {
+  if (variant < 0 || variant >= kDirectColVariants) return cudaErrorInvalidValue;
+  const DirectCols& d = kDirectCols[variant];
+  GroupDesc g = gd;
+  set_divisors(g);
+  const int np = d.r[2] > 0 ? 3 : 2;
+  bool ok = g.M == d.M && g.npass == np && g.nsub >= 1;
+  for (int t = 0; t < np && ok; ++t) ok = g.pass[t].R == d.r[t] && (t == 0) == (g.pass[t].tw == nullptr);
+  if (!ok) return cudaErrorInvalidValue;
+  const int64_t ntiles = (g.total_sub + 15) / 16;
+  if (ntiles == 0) return cudaSuccess;
+  if (ntiles > 0x7fffffff) return cudaErrorInvalidValue;
+  const DirectFn kern = fwd ? direct_cols_fn<true>(variant) : direct_cols_fn<false>(variant);
+  kern<<<(unsigned)ntiles, d.M, direct_cols_smem(variant), stream>>>(
+      g, static_cast<const float2*>(in), static_cast<float2*>(out));
+  return cudaGetLastError();
+}
+
 cudaError_t prepare_direct_kernels_f32() {
+  for (int v = 0; v < kDirectColVariants; ++v) {
+    const int bytes = (int)direct_cols_smem(v);
+    cudaError_t e = cudaFuncSetAttribute(direct_cols_fn<true>(v),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(direct_cols_fn<false>(v), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bytes);
+    if (e != cudaSuccess) return e;
+  }
   for (int v = 0; v < kDirectVariants; ++v) {
     const int bytes = (int)direct_smem(v);
     cudaError_t e = cudaFuncSetAttribute(direct_fn<true>(v),

@@ -82,6 +82,13 @@ cudaError_t launch_tile_stream_f32(const GroupDesc& g, bool fwd, const void* in,
 enum DirectLayoutKind { kDirectFirstOfTwo = 0, kDirectSecondOfTwo = 1, kDirectSingle = 2 };
 int direct_variant_f32(int layout, int M, int nsub, bool comp, const int* radices, int npass);
 cudaError_t prepare_direct_kernels_f32();
+// The columns of a batch of images (a group whose sub-problems are the columns: line = image,
+// in_sub / out_sub = column step, in_elem / out_elem = row step; tiles may straddle images):
+// the register-staged kernel of direct_cols_variant_f32 (power-of-two M = 64 .. 512 with
+// radices 16.4, 16.8, 16.16, 16.16.2), or -1.
+int direct_cols_variant_f32(int M, const int* radices, int npass);
+cudaError_t launch_direct_cols_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
+                                   int variant, cudaStream_t stream);
 cudaError_t launch_direct_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                               int variant, cudaStream_t stream);
 

@@ -100,6 +100,7 @@ struct Plan {
   // tables are then in pass order rather than transposed.
   int direct_variant[2] = {-1, -1};
   unsigned col_ts_grid = 0;     // binary32 column pass of a rank-2 real plan: persistent grid
+  int col_direct = -1;          // ... or its register-staged column kernel (-1: none)
   int* d_status = nullptr; // set to 1 on the device when a bounded wait gave up
   bool wait_give_up = false;  // LFG_TEST_WAIT_GIVE_UP: tile waits give up at once (tests)
   bool generic_kernels = false;  // LFG_GENERIC_KERNELS: no compile-time kernel variants

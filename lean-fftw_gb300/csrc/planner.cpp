@@ -660,6 +660,10 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
   int64_t cmax = std::max<int64_t>(1, tile_target / std::max<int64_t>(M, 1));
   while (cmax > 1 && smem_bytes(cmax, M, prec) > kSmemBudget) --cmax;
   d.g.C = (int)std::min<int64_t>(cmax, std::max<int64_t>(1, d.lines));
+  // binary32 r2c rows of a power-of-two size with a register-staged kernel
+  d.direct = prec == 1 && r2c && !p.generic_kernels && M >= 2
+                 ? r2c_rows_variant_f32((int)M, p.radices.data(), (int)p.radices.size())
+                 : -1;
   // split twiddles cos/sin(2 pi k / N), k = 0..M/2, halved for r2c
   std::vector<double> tab = cos_sin_2pi_table((uint64_t)N);
   // [halved table | full table]
@@ -719,6 +723,10 @@ std::string build_real(Plan& p, const RealLayout& L, int64_t tile_target) {
       d.c_rdist = h;
     }
     p.flops += plan_ops(L.n0, crs) * (double)(L.howmany * h);
+    // binary32 columns of a power-of-two length: the register-staged column kernel
+    p.col_direct = prec == 1 && !p.generic_kernels
+                       ? direct_cols_variant_f32((int)L.n0, crs.data(), (int)crs.size())
+                       : -1;
     // binary32 columns: the persistent strided-tile kernel (the next tile's elements copied
     // asynchronously under the current tile's passes) when its three tile buffers fit
     if (prec == 1 && smem_bytes(g.C, g.M, prec) / 2 * 3 <= kSmemBudget) {
@@ -834,6 +842,7 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
   const size_t es = p.precision == 0 ? 16 : 8;
   auto launch_col = [&](bool fwd, const void* a, void* b) -> cudaError_t {
     if (p.precision == 0) return launch_group_f64(p.col, fwd, a, b, stream);
+    if (p.col_direct >= 0) return launch_direct_cols_f32(p.col, fwd, a, b, p.col_direct, stream);
     if (p.col_ts_grid && ((uintptr_t)a % 8) == 0 && ((uintptr_t)b % 8) == 0)
       return launch_tile_stream_f32(p.col, fwd, a, b, p.col_ts_grid, stream);
     return launch_group_f32(p.col, fwd, a, b, stream);

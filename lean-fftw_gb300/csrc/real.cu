@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 
 #include "real.h"
+
+#include "direct_dev.cuh"
 #include "stockham_dev.cuh"
 
 namespace lfg {
@@ -148,6 +150,89 @@ c2r_kernel(const RealDesc d, const typename Prec<T>::C* in, T* out) {
   }
 }
 
+// The rows of a binary32 r2c plan with a register-staged variant (M = N / 2 complex points a
+// power of two): C = 4096 / M rows per CTA of 256 threads; the first pass loads its
+// butterflies' inputs straight from the rows, the later passes run through shared tiles, and
+// the split epilogue reads the last tile and stores the half spectrum -- the operations of
+// r2c_kernel above on the same operands, so the same bits.
+template <int M, int R0, int R1, int R2>
+__global__ void __launch_bounds__(256, 3)
+r2c_rows_direct_f32(const RealDesc d, const float* in, float2* out) {
+  using namespace dfx;
+  using P = Prec<float>;
+  const RealOps<float> ops;
+  constexpr int C = kDirectPoints / M, T = 256, PM = sub_pitch(M), MR0 = M / R0;
+  static_assert(M == R0 * R1 * (R2 > 0 ? R2 : 1) && C * MR0 == T, "one first-pass butterfly per thread");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* A = reinterpret_cast<float2*>(smem_raw);
+  float2* B = A + C * PM;
+  const GroupDesc& g = d.g;
+  const int64_t l0 = (int64_t)blockIdx.x * C;
+  const int count = (int)min((int64_t)C, d.lines - l0);
+  const int c0 = (int)threadIdx.x / MR0;   // the thread's row in the first pass
+  const bool valid = c0 < count;
+  const float2* tin = valid ? reinterpret_cast<const float2*>(in + real_base(d, l0 + c0)) : nullptr;
+  direct_pass<true, M, C, PM, T, R0, 1, 0, false, 0, kFromRowsRT, kToTile>(
+      nullptr, 0, nullptr, A, nullptr, 0, nullptr, 0, count, true, 1.0f, tin, nullptr, 0, valid);
+  __syncthreads();
+  direct_pass<true, M, C, PM, T, R1, R0, 0, false, 1, kFromTile, kToTile>(
+      nullptr, 0, A, B, nullptr, 0, static_cast<const float2*>(g.pass[1].tw), 0, count, true, 1.0f);
+  __syncthreads();
+  const float2* F = B;
+  if constexpr (R2 > 0) {
+    direct_pass<true, M, C, PM, T, R2, R0 * R1, 0, false, 1, kFromTile, kToTile>(
+        nullptr, 0, B, A, nullptr, 0, static_cast<const float2*>(g.pass[2].tw), 0, count, true,
+        1.0f);
+    __syncthreads();
+    F = A;
+  }
+  const float2* __restrict__ tw = static_cast<const float2*>(d.adjoint ? d.post_full : d.post);
+  const float hf = d.adjoint ? 1.0f : 0.5f;
+  constexpr int half = M / 2;
+  for (int idx = threadIdx.x; idx < count * (half + 1); idx += T) {
+    const int c = idx / (half + 1), k = idx - c * (half + 1);
+    const float2* Fc = F + c * PM;
+    float2* o = out + cplx_base(d, l0 + c);
+    if (k == 0) {
+      const float2 z = Fc[0];
+      o[0] = P::mk(ops.add(z.x, z.y), 0.0f);
+      o[M] = P::mk(ops.sub(z.x, z.y), 0.0f);
+      continue;
+    }
+    const float2 a = Fc[spad(k)], bc = Fc[spad(M - k)];
+    const float sr = ops.add(a.x, bc.x), si = ops.sub(a.y, bc.y);
+    const float dr = ops.sub(a.x, bc.x), di = ops.add(a.y, bc.y);
+    const float2 w = __ldg(tw + k);
+    const float Pp = P::fma(w.x, di, -ops.mul(w.y, dr));
+    const float Q = P::fma(w.y, di, ops.mul(w.x, dr));
+    o[k] = P::mk(P::fma(hf, sr, Pp), P::fma(hf, si, -Q));
+    if (k != M - k) o[M - k] = P::mk(P::fma(hf, sr, -Pp), P::fma(-hf, si, -Q));
+  }
+}
+
+using RowsFn = void (*)(const RealDesc, const float*, float2*);
+struct RowsVariant {
+  int M, r[3];
+};
+constexpr RowsVariant kRowsVariants[] = {
+    {128, {16, 8, 0}}, {256, {16, 16, 0}}, {512, {16, 16, 2}}, {1024, {16, 16, 4}}};
+constexpr int kNRowsVariants = (int)(sizeof(kRowsVariants) / sizeof(kRowsVariants[0]));
+
+RowsFn rows_fn(int v) {
+  switch (v) {
+    case 0: return r2c_rows_direct_f32<128, 16, 8, 0>;
+    case 1: return r2c_rows_direct_f32<256, 16, 16, 0>;
+    case 2: return r2c_rows_direct_f32<512, 16, 16, 2>;
+    case 3: return r2c_rows_direct_f32<1024, 16, 16, 4>;
+    default: return nullptr;
+  }
+}
+
+size_t rows_smem(int v) {
+  const int M = kRowsVariants[v].M;
+  return 2 * (size_t)(dfx::kDirectPoints / M) * sub_pitch(M) * sizeof(float2);
+}
+
 template <class K>
 cudaError_t allow_max_smem(K kern) {
   cudaFuncAttributes a;
@@ -166,7 +251,12 @@ cudaError_t launch_real_t(const RealDesc& rd, bool r2c, const void* in, void* ou
   const int64_t grid = (d.lines + d.g.C - 1) / d.g.C;
   if (grid <= 0) return cudaSuccess;
   const size_t smem = 2 * (size_t)tile_elems(d.g.C, d.M) * sizeof(Cx);
-  if (r2c)
+  if (r2c && sizeof(T) == 4 && d.direct >= 0 && d.direct < kNRowsVariants) {
+    const int C = dfx::kDirectPoints / kRowsVariants[d.direct].M;
+    const int64_t tiles = (d.lines + C - 1) / C;
+    rows_fn(d.direct)<<<(unsigned)tiles, 256, rows_smem(d.direct), stream>>>(
+        d, reinterpret_cast<const float*>(in), reinterpret_cast<float2*>(out));
+  } else if (r2c)
     r2c_kernel<T><<<(unsigned)grid, kGroupThreads, smem, stream>>>(
         d, static_cast<const T*>(in), static_cast<Cx*>(out));
   else
@@ -177,11 +267,26 @@ cudaError_t launch_real_t(const RealDesc& rd, bool r2c, const void* in, void* ou
 
 }  // namespace
 
+int r2c_rows_variant_f32(int M, const int* radices, int npass) {
+  for (int v = 0; v < kNRowsVariants; ++v) {
+    const RowsVariant& rv = kRowsVariants[v];
+    if (rv.M != M || (rv.r[2] > 0 ? 3 : 2) != npass) continue;
+    bool same = true;
+    for (int t = 0; t < npass; ++t) same = same && rv.r[t] == radices[t];
+    if (same) return v;
+  }
+  return -1;
+}
+
 cudaError_t prepare_real_kernels() {
   cudaError_t e;
   if ((e = allow_max_smem(r2c_kernel<double>)) != cudaSuccess) return e;
   if ((e = allow_max_smem(c2r_kernel<double>)) != cudaSuccess) return e;
   if ((e = allow_max_smem(r2c_kernel<float>)) != cudaSuccess) return e;
+  for (int v = 0; v < kNRowsVariants; ++v)
+    if ((e = cudaFuncSetAttribute(rows_fn(v), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)rows_smem(v))) != cudaSuccess)
+      return e;
   return allow_max_smem(c2r_kernel<float>);
 }
 

@@ -25,9 +25,14 @@ struct RealDesc {
   // its output (the gradient of c2r); c2r halves the bins 1..M-1 of its input (the gradient
   // of r2c).  0 = plain transform.
   int adjoint;
+  // binary32 r2c rows: the register-staged kernel of r2c_rows_variant_f32 (-1: r2c_kernel)
+  int direct = -1;
 };
 
 cudaError_t prepare_real_kernels();
+// The register-staged binary32 r2c row kernel for M = N / 2 points with these radices
+// (128: 16.8, 256: 16.16, 512: 16.16.2, 1024: 16.16.4), or -1.
+int r2c_rows_variant_f32(int M, const int* radices, int npass);
 // precision 0: binary64 (double lines, double2 spectrum); 1: binary32 (float, float2)
 cudaError_t launch_real(const RealDesc& d, int precision, bool r2c, const void* in, void* out,
                         cudaStream_t stream);

@@ -110,13 +110,15 @@ def plan_1d(n: int, sign: int = -1, howmany: int = 1, precision="f64",
     return Plan(h)
 
 
-def plan_r2c(n: int, howmany: int = 1, precision="f64", adjoint: bool = False) -> Plan:
+def plan_r2c(n: int, howmany: int = 1, precision="f64", adjoint: bool = False,
+             generic_kernels: bool = False) -> Plan:
     """Real forward transform of even size n on `howmany` contiguous lines: n doubles in,
     n/2+1 complex out per line (the generic engine's r2c, Core/Problem.lean:145-147).
-    adjoint=True doubles output bins 1..n/2-1: the gradient of c2r."""
+    adjoint=True doubles output bins 1..n/2-1: the gradient of c2r.  generic_kernels: run
+    the kernels with runtime pass descriptors (the same bits)."""
     h = ctypes.c_void_p()
-    check(lib().lfg_plan_r2c(n, howmany, _prec(precision), _lib.LFG_ADJOINT if adjoint else 0,
-                             ctypes.byref(h)))
+    flags = (_lib.LFG_ADJOINT if adjoint else 0) | (_lib.LFG_GENERIC_KERNELS if generic_kernels else 0)
+    check(lib().lfg_plan_r2c(n, howmany, _prec(precision), flags, ctypes.byref(h)))
     return Plan(h)
 
 
@@ -143,17 +145,22 @@ def plan_r2r(n: int, kind, howmany: int = 1, precision="f64") -> Plan:
     return Plan(h)
 
 
-def plan_r2c_2d(n0: int, n1: int, howmany: int = 1, precision="f64") -> Plan:
-    """Rank-2 r2c of n0 x n1 real images to n0 x (n1/2+1) complex (Core/Problem.lean:228-233)."""
+def plan_r2c_2d(n0: int, n1: int, howmany: int = 1, precision="f64",
+                generic_kernels: bool = False) -> Plan:
+    """Rank-2 r2c of n0 x n1 real images to n0 x (n1/2+1) complex (Core/Problem.lean:228-233).
+    generic_kernels: run the kernels with runtime pass descriptors (the same bits)."""
     h = ctypes.c_void_p()
-    check(lib().lfg_plan_r2c_2d(n0, n1, howmany, _prec(precision), 0, ctypes.byref(h)))
+    check(lib().lfg_plan_r2c_2d(n0, n1, howmany, _prec(precision),
+                                _lib.LFG_GENERIC_KERNELS if generic_kernels else 0, ctypes.byref(h)))
     return Plan(h)
 
 
-def plan_c2r_2d(n0: int, n1: int, howmany: int = 1, precision="f64") -> Plan:
+def plan_c2r_2d(n0: int, n1: int, howmany: int = 1, precision="f64",
+                generic_kernels: bool = False) -> Plan:
     """Rank-2 c2r: complex backward along the first axis, then c2r along the last."""
     h = ctypes.c_void_p()
-    check(lib().lfg_plan_c2r_2d(n0, n1, howmany, _prec(precision), 0, ctypes.byref(h)))
+    check(lib().lfg_plan_c2r_2d(n0, n1, howmany, _prec(precision),
+                                _lib.LFG_GENERIC_KERNELS if generic_kernels else 0, ctypes.byref(h)))
     return Plan(h)
 
 

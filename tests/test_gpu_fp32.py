@@ -117,6 +117,51 @@ def test_two_group_variants_equal_generic_kernels(n, sign, comp):
     assert torch.equal(c, a)
 
 
+@pytest.mark.parametrize("n,B", [(256, 37), (512, 64), (1024, 9), (2048, 5), (4096, 3), (600, 7)])
+def test_real_rows_register_staged_equal_generic(n, B):
+    """Binary32 r2c rows of a power-of-two size with a register-staged kernel (first pass from
+    the rows, split epilogue from the last shared tile) give the generic kernel's bits; the
+    batch leaves a partial last tile; a size without such a kernel (600) is unaffected."""
+    x = torch.from_numpy(np.random.default_rng(n).random((B, n)).astype(np.float32) - 0.5).cuda()
+    fast, slow = lfg.plan_r2c(n, B, precision="f32"), lfg.plan_r2c(n, B, precision="f32", generic_kernels=True)
+    yf = torch.empty(B, n // 2 + 1, dtype=torch.complex64, device="cuda")
+    ys = torch.empty_like(yf)
+    fast.execute(x, yf)
+    slow.execute(x, ys)
+    torch.cuda.synchronize()
+    assert torch.equal(torch.view_as_real(yf), torch.view_as_real(ys)), n
+
+
+@pytest.mark.parametrize("n0,n1,B", [(512, 512, 3), (256, 256, 2), (64, 1024, 2), (128, 128, 5),
+                                     (100, 512, 2), (512, 60, 2)])
+def test_real_2d_register_staged_equal_generic(n0, n1, B):
+    """Binary32 rank-2 r2c and c2r: the register-staged row kernel and column kernel (16
+    columns per tile, tiles straddling images; power-of-two column lengths 64 .. 512) give
+    the generic kernels' bits in both directions."""
+    x = torch.from_numpy(np.random.default_rng(n0 + n1).random((B, n0, n1)).astype(np.float32)
+                         - 0.5).cuda()
+    h = n1 // 2 + 1
+    fast = lfg.plan_r2c_2d(n0, n1, B, precision="f32")
+    slow = lfg.plan_r2c_2d(n0, n1, B, precision="f32", generic_kernels=True)
+    yf = torch.empty(B, n0, h, dtype=torch.complex64, device="cuda")
+    ys = torch.empty_like(yf)
+    fast.execute(x, yf)
+    slow.execute(x, ys)
+    torch.cuda.synchronize()
+    assert torch.equal(torch.view_as_real(yf), torch.view_as_real(ys)), (n0, n1)
+    cf = lfg.plan_c2r_2d(n0, n1, B, precision="f32")
+    cs = lfg.plan_c2r_2d(n0, n1, B, precision="f32", generic_kernels=True)
+    zf = torch.empty(B, n0, n1, dtype=torch.float32, device="cuda")
+    zs = torch.empty_like(zf)
+    cf.execute(yf.clone(), zf)
+    cs.execute(yf.clone(), zs)
+    torch.cuda.synchronize()
+    assert torch.equal(zf, zs), (n0, n1)
+    # and the round trip is the identity up to binary32 rounding (scale n0 * n1)
+    e = float(torch.linalg.vector_norm(zf / (n0 * n1) - x) / torch.linalg.vector_norm(x))
+    assert e < 1e-5, e
+
+
 @pytest.mark.parametrize("n", [1 << 16, 1 << 17, 1 << 18])
 def test_compensation_helps_large_sizes(n):
     """Compensated (hi, lo) twiddle products in the last passes remove the twiddles' own
