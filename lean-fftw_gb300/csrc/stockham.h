@@ -15,8 +15,9 @@
 //     stride-N/P subsequence x[b + (N/P) i], written contiguously to z[b*P + m];
 //   * second group (passes T..s-1): sub-problem m < P is the stride-P subsequence
 //     z[q*P + m]; it is read and written in place, and the table index of a twiddle is
-//     k = k_local*P + m (the planner stores these tables transposed, at m*ns_local + k_local,
-//     so that a warp's threads, which walk k_local, read neighbouring entries).
+//     k = k_local*P + m (for the shared-memory group kernels the planner stores these tables
+//     transposed, at m*ns_local + k_local, so that a warp's threads, which walk k_local, read
+//     neighbouring entries; the binary32 register-staged kernels walk m and keep pass order).
 //
 // Both facts follow from the pass formula: after passes 0..T-1, positions b*P..b*P+P-1 hold
 // the size-P transform of x[b + (N/P) i]; every later pass maps positions = m (mod P) to
