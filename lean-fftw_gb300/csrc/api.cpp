@@ -1133,6 +1133,7 @@ static lfg_status lfg_get_plan_info_impl(const lfg_plan* plan, lfg_plan_info* in
   info->flops = p.flops;
   info->cluster_ctas = p.cluster ? p.cluster_args.S : 0;
   info->direct_groups = (p.direct_variant[0] >= 0) + (p.direct_variant[1] >= 0);
+  info->small_kernel = p.small_grid ? 1 : 0;
   return LFG_OK;
 }
 

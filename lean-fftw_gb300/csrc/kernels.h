@@ -92,6 +92,16 @@ cudaError_t launch_direct_cols_f32(const GroupDesc& g, bool fwd, const void* in,
 cudaError_t launch_direct_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                               int variant, cudaStream_t stream);
 
+// Batched one-butterfly transforms (a single untwiddled pass of R = N <= kSmallMaxN points,
+// one sub-problem per line), binary64 or binary32 (precision 0 / 1): the warp-tile kernel of
+// small.cu, one per precision, direction and R.
+constexpr int kSmallMaxN = 16;
+bool small_kernel_applies(const GroupDesc& g);
+cudaError_t prepare_small_kernels();
+unsigned small_grid(const GroupDesc& g, int precision);
+cudaError_t launch_small(const GroupDesc& g, int precision, bool fwd, const void* in, void* out,
+                         unsigned grid, cudaStream_t stream);
+
 // Persistent FP64 kernel over a ragged batch (one launch for all sizes), in kRaggedVariants
 // block shapes (threads x minimum CTAs per SM).
 constexpr int kRaggedVariants = 5;

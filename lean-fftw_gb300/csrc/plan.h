@@ -99,6 +99,8 @@ struct Plan {
   // (direct_f32.cu; -1: none).  Set for both groups or neither; the second group's twiddle
   // tables are then in pass order rather than transposed.
   int direct_variant[2] = {-1, -1};
+  unsigned small_grid = 0;      // one-butterfly sizes (N <= 16): the warp-tile kernel's grid
+                                // (small.cu; 0: not used)
   unsigned col_ts_grid = 0;     // binary32 column pass of a rank-2 real plan: persistent grid
   int col_direct = -1;          // ... or its register-staged column kernel (-1: none)
   int* d_status = nullptr; // set to 1 on the device when a bounded wait gave up

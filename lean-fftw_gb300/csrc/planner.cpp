@@ -35,6 +35,22 @@ static bool direct_enabled() {
   return !(s && s[0] == '0');
 }
 
+// LFG_SMALL=0 in the environment (read at planning): one-butterfly sizes run on the group or
+// bulk-copy kernels instead of the warp-tile kernel (for comparisons; the same bits).
+static bool small_enabled() {
+  const char* s = std::getenv("LFG_SMALL");
+  return !(s && s[0] == '0');
+}
+
+// Where the warp-tile kernel runs a one-butterfly size, from 1 GiB batches on GB300: binary64
+// N <= 15 (1.1-2.1x the group kernel; N = 16 spills and is 5 % slower); binary32 every N
+// except, where the persistent bulk-copy kernel takes the plan (back-to-back lines, N even),
+// N = 2, 4, 6, 10 and 12, which that kernel runs at 0.85-0.98 of HBM against 0.74-0.86.
+static bool small_preferred(int prec, int64_t N, bool bulk_copy) {
+  if (prec == 0) return N <= 15;
+  return !(bulk_copy && (N == 2 || N == 4 || N == 6 || N == 10 || N == 12));
+}
+
 namespace {
 
 // per-point operations of a twiddled pass of radix R
@@ -589,6 +605,13 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
       p.direct_variant[0] = direct_variant_f32(kDirectSingle, (int)N, 1, false, rs.data(),
                                                (int)rs.size());
   }
+  // one-butterfly sizes (N <= 16, one untwiddled pass): the warp-tile kernel, ahead of the
+  // group and bulk-copy kernels
+  p.small_grid = 0;
+  if (p.ngroups == 1 && p.howmany2 == 1 && p.stages.empty() && p.howmany > 0 && !p.cluster &&
+      !p.generic_kernels && !p.wait_give_up && small_enabled() && small_kernel_applies(g0) &&
+      small_preferred(prec, N, p.stream) && prepare_small_kernels() == cudaSuccess)
+    p.small_grid = small_grid(g0, prec);
   if (prec == 1 && !p.stream && p.howmany > 0) {
     // three tile buffers per CTA (stage + two work buffers): shrink C to fit
     int dev = 0, sms = 1;
@@ -884,6 +907,8 @@ cudaError_t execute_plan(const Plan& p, const void* in, void* out, cudaStream_t 
       return launch_direct_f32(p.groups[0], p.fwd, ib, ob, p.direct_variant[0], stream);
     if (p.cluster && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)
       return launch_cluster_f64(p.cluster_args, p.groups[0].scale, ib, ob, stream);
+    if (p.small_grid)
+      return launch_small(p.groups[0], p.precision, p.fwd, ib, ob, p.small_grid, stream);
     // the bulk-copy engine needs 16-byte aligned ranges; in place is fine (each tile is read
     // into shared memory before it is written)
     if (p.stream && ((uintptr_t)ib % 16) == 0 && ((uintptr_t)ob % 16) == 0)

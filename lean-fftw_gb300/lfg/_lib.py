@@ -37,7 +37,8 @@ class PlanInfo(ctypes.Structure):
                 ("precision", ctypes.c_int), ("npass", ctypes.c_int), ("ngroups", ctypes.c_int),
                 ("radices", ctypes.c_int * 24), ("in_bytes", ctypes.c_int64),
                 ("out_bytes", ctypes.c_int64), ("flops", ctypes.c_double),
-                ("cluster_ctas", ctypes.c_int), ("direct_groups", ctypes.c_int)]
+                ("cluster_ctas", ctypes.c_int), ("direct_groups", ctypes.c_int),
+                ("small_kernel", ctypes.c_int)]
 
 
 class LfgError(RuntimeError):
