@@ -9,8 +9,8 @@
 //   1. the chunk (32 K transforms, K = 256 / (R x element bytes), so that every lane has about
 //      256 bytes in flight) is read with coalesced loads -- consecutive lanes take consecutive elements
 //      of a transform when elements are contiguous, else the same element of consecutive
-//      transforms -- into the warp's tile, transform t at t * PT (PT = R | 1, odd, so that
-//      lane-strided accesses of 8 or 16 bytes fall on distinct banks);
+//      transforms -- into the warp's tile (layout: small_slot below, conflict-free for the
+//      staging and for the lane-strided reads and writes of step 2);
 //   2. each lane runs the codelet on K transforms of the tile, in place (scaled on the way
 //      out when the plan's scale is not 1, as the group kernel's stores do);
 //   3. the chunk is written back with the loads' ordering.
@@ -37,14 +37,33 @@ constexpr int kSmallWarps = kSmallThreads / 32;
 __host__ __device__ constexpr int small_k(int R, int elem_bytes) {
   return R * elem_bytes >= 256 ? 1 : 256 / (R * elem_bytes);
 }
-__host__ __device__ constexpr int small_pitch(int R) { return R | 1; }
+// Tile layout: transform t's element r at t * pitch + slot(t, r).  Binary64 with power-of-two
+// R: no padding, the element index XOR-swizzled by a function of t so that both the staging
+// accesses (consecutive elements) and the per-lane reads (one transform per lane, stride R)
+// hit distinct banks (N = 2: 0.430 -> 0.367 ms with the 3-CTA register cap below).  Otherwise
+// an odd pitch R | 1 and no swizzle (binary32 measured slower swizzled: N = 8 0.403 -> 0.449
+// ms, the extra index arithmetic spilling at the 128-register cap).
+__host__ __device__ constexpr bool small_swizzled(int R, int elem_bytes) {
+  return elem_bytes == 16 && (R & (R - 1)) == 0;
+}
+__host__ __device__ constexpr int small_pitch(int R, int elem_bytes) {
+  return small_swizzled(R, elem_bytes) ? R : (R | 1);
+}
+// U = 128-byte bank row / element size: the accesses of one shared-memory wavefront
+template <int R, int U>
+__device__ __forceinline__ int small_slot(int t, int r) {
+  if constexpr (small_swizzled(R, 128 / U)) return r ^ ((t / (U > R ? U / R : 1)) & (R - 1));
+  else return r;
+}
 
+// binary64 R <= 8: three CTAs per SM (80 registers, no spills; more loads in flight), else two
 template <class T, bool FWD, int R>
-__global__ void __launch_bounds__(kSmallThreads, 2)
+__global__ void __launch_bounds__(kSmallThreads, (sizeof(T) == 8 && R <= 8) ? 3 : 2)
 small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>::C* out) {
   using P = Prec<T>;
   using Cx = typename P::C;
-  constexpr int K = small_k(R, (int)sizeof(Cx)), TPW = 32 * K, PT = small_pitch(R);
+  constexpr int K = small_k(R, (int)sizeof(Cx)), TPW = 32 * K, PT = small_pitch(R, (int)sizeof(Cx));
+  constexpr int U = 128 / (int)sizeof(Cx);
   extern __shared__ double2 small_smem[];
   const int lane = threadIdx.x & 31;
   Cx* const tile = reinterpret_cast<Cx*>(small_smem) + (threadIdx.x >> 5) * (TPW * PT);
@@ -67,7 +86,7 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
 #pragma unroll
       for (int k = 0; k < R * K; ++k) {
         const int e = k * 32 + lane;
-        if (e < nt * R) tile[(e / R) * PT + e % R] = src[e];
+        if (e < nt * R) tile[(e / R) * PT + small_slot<R, U>(e / R, e % R)] = src[e];
       }
     } else {
 #pragma unroll
@@ -75,31 +94,33 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
         const int e = k * 32 + lane;
         const int t = in_rfast ? e / R : e % TPW;
         const int r = in_rfast ? e - t * R : e / TPW;
-        if (t < nt) tile[t * PT + r] = src[(int64_t)t * il + (int64_t)r * ie];
+        if (t < nt) tile[t * PT + small_slot<R, U>(t, r)] = src[(int64_t)t * il + (int64_t)r * ie];
       }
     }
     __syncwarp();
 #pragma unroll 1
     for (int k = 0; k < K; ++k) {
-      Cx* const v = tile + (k * 32 + lane) * PT;
+      const int t = k * 32 + lane;
+      Cx* const v = tile + t * PT;
       T x[2 * R], y[2 * R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const Cx a = v[r];
+        const Cx a = v[small_slot<R, U>(t, r)];
         x[2 * r] = a.x;
         x[2 * r + 1] = a.y;
       }
       P::template Bfly<FWD, R, false>::run(x, y, one, nz);
 #pragma unroll
       for (int r = 0; r < R; ++r)
-        v[r] = unit ? P::mk(y[2 * r], y[2 * r + 1]) : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
+        v[small_slot<R, U>(t, r)] = unit ? P::mk(y[2 * r], y[2 * r + 1])
+                                         : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
     }
     __syncwarp();
     if (out_packed) {
 #pragma unroll
       for (int k = 0; k < R * K; ++k) {
         const int e = k * 32 + lane;
-        if (e < nt * R) dst[e] = tile[(e / R) * PT + e % R];
+        if (e < nt * R) dst[e] = tile[(e / R) * PT + small_slot<R, U>(e / R, e % R)];
       }
     } else {
 #pragma unroll
@@ -107,7 +128,7 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
         const int e = k * 32 + lane;
         const int t = out_rfast ? e / R : e % TPW;
         const int r = out_rfast ? e - t * R : e / TPW;
-        if (t < nt) dst[(int64_t)t * ol + (int64_t)r * oe] = tile[t * PT + r];
+        if (t < nt) dst[(int64_t)t * ol + (int64_t)r * oe] = tile[t * PT + small_slot<R, U>(t, r)];
       }
     }
     __syncwarp();   // the tile is refilled by the warp's next chunk
@@ -117,7 +138,7 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
 template <class T>
 size_t small_smem(int R) {
   constexpr int es = (int)sizeof(typename Prec<T>::C);
-  return (size_t)kSmallWarps * 32 * small_k(R, es) * small_pitch(R) * es;
+  return (size_t)kSmallWarps * 32 * small_k(R, es) * small_pitch(R, es) * es;
 }
 
 template <class T, bool FWD>
