@@ -43,11 +43,11 @@ static bool small_enabled() {
 }
 
 // Where the warp-tile kernel runs a one-butterfly size, from 1 GiB batches on GB300: binary64
-// N <= 15 (1.1-2.1x the group kernel; N = 16 spills and is 5 % slower); binary32 every N
-// except, where the persistent bulk-copy kernel takes the plan (back-to-back lines, N even),
-// N = 2, 4, 6, 10 and 12, which that kernel runs at 0.85-0.98 of HBM against 0.74-0.86.
+// every N (1.04-2.2x the group kernel); binary32 every N except, where the persistent
+// bulk-copy kernel takes the plan (back-to-back lines, N even), N = 2, 4, 6, 10 and 12, which
+// that kernel runs at 0.85-0.98 of HBM against 0.74-0.86.
 static bool small_preferred(int prec, int64_t N, bool bulk_copy) {
-  if (prec == 0) return N <= 15;
+  if (prec == 0) return true;
   return !(bulk_copy && (N == 2 || N == 4 || N == 6 || N == 10 || N == 12));
 }
 

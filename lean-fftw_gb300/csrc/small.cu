@@ -56,9 +56,12 @@ __device__ __forceinline__ int small_slot(int t, int r) {
   else return r;
 }
 
-// binary64 R <= 8: three CTAs per SM (80 registers, no spills; more loads in flight), else two
+// binary64 R <= 8: three CTAs per SM (80 registers, no spills; more loads in flight); binary64
+// R = 16: one (224 registers; at 128 it spills, and 4 % slower than the group kernel, 1.163
+// against 1.213 ms for 2^22 lines); else two
 template <class T, bool FWD, int R>
-__global__ void __launch_bounds__(kSmallThreads, (sizeof(T) == 8 && R <= 8) ? 3 : 2)
+__global__ void __launch_bounds__(kSmallThreads,
+                                  (sizeof(T) == 8 && R <= 8) ? 3 : (sizeof(T) == 8 && R == 16) ? 1 : 2)
 small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>::C* out) {
   using P = Prec<T>;
   using Cx = typename P::C;

@@ -23,10 +23,10 @@ SIZES = list(range(2, 17))
 
 
 def _expect_small(n, precision):
-    """The planner's choice for back-to-back lines: binary64 N <= 15; binary32 all but the
+    """The planner's choice for back-to-back lines: binary64 every N; binary32 all but the
     sizes the bulk-copy kernel runs faster (N = 2, 4, 6, 10, 12)."""
     if precision == "f64":
-        return int(n <= 15)
+        return 1
     return int(n not in (2, 4, 6, 10, 12))
 
 
@@ -59,7 +59,7 @@ def test_small_sizes_match_group_kernel_and_oracle(n, precision):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-@pytest.mark.parametrize("n", [3, 8, 13, 15])
+@pytest.mark.parametrize("n", [3, 8, 13, 15, 16])
 def test_small_sizes_scaled(n, precision):
     B = 999
     x = O.uniform_complex((B, n), seed=n)
@@ -71,7 +71,7 @@ def test_small_sizes_scaled(n, precision):
     assert _bits_equal(plan.execute(xd), generic.execute(xd)), n
 
 
-@pytest.mark.parametrize("n", [2, 5, 8, 15])
+@pytest.mark.parametrize("n", [2, 5, 8, 15, 16])
 def test_small_sizes_strided_layouts(n):
     """Lines dist = n + 3 apart (gapped: the element-contiguous order without the packed fast
     path) and lines interleaved (stride B, dist 1: the line-contiguous order), binary64,
