@@ -170,7 +170,8 @@ typedef struct {
   double flops;         /* binary64 instructions of the codelets per execution */
   int cluster_ctas;     /* a lone transform on a thread-block cluster: its CTAs (0: none) */
   int direct_groups;    /* binary32 groups run by the register-staged two-pass kernel   */
-  int small_kernel;     /* 1: a one-butterfly size (n <= 16) run by the warp-tile kernel */
+  int small_kernel;     /* 1: run by the warp-tile kernel (one butterfly, n <= 16, or a
+                         * binary32 two-pass plan of n <= 32)                            */
 } lfg_plan_info;
 
 lfg_status lfg_get_plan_info(const lfg_plan *plan, lfg_plan_info *info);

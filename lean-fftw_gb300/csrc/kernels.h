@@ -92,11 +92,12 @@ cudaError_t launch_direct_cols_f32(const GroupDesc& g, bool fwd, const void* in,
 cudaError_t launch_direct_f32(const GroupDesc& g, bool fwd, const void* in, void* out,
                               int variant, cudaStream_t stream);
 
-// Batched one-butterfly transforms (a single untwiddled pass of R = N <= kSmallMaxN points,
-// one sub-problem per line), binary64 or binary32 (precision 0 / 1): the warp-tile kernel of
-// small.cu, one per precision, direction and R.
+// Batched small transforms on the warp-tile kernel of small.cu (one sub-problem per line):
+// one untwiddled pass of R = N <= kSmallMaxN points, binary64 or binary32 (precision 0 / 1),
+// or two passes of a binary32 plan of N <= kSmallMaxTwoPassN points with a compiled radix pair.
 constexpr int kSmallMaxN = 16;
-bool small_kernel_applies(const GroupDesc& g);
+constexpr int kSmallMaxTwoPassN = 32;
+bool small_kernel_applies(const GroupDesc& g, int precision);
 cudaError_t prepare_small_kernels();
 unsigned small_grid(const GroupDesc& g, int precision);
 cudaError_t launch_small(const GroupDesc& g, int precision, bool fwd, const void* in, void* out,

@@ -42,12 +42,16 @@ static bool small_enabled() {
   return !(s && s[0] == '0');
 }
 
-// Where the warp-tile kernel runs a one-butterfly size, from 1 GiB batches on GB300: binary64
-// every N (1.04-2.2x the group kernel); binary32 every N except, where the persistent
-// bulk-copy kernel takes the plan (back-to-back lines, N even), N = 2, 4, 6, 10 and 12, which
-// that kernel runs at 0.85-0.98 of HBM against 0.74-0.86.
-static bool small_preferred(int prec, int64_t N, bool bulk_copy) {
+// Where the warp-tile kernel runs a plan it has a variant for, from 1 GiB batches on GB300:
+// binary64 one-butterfly sizes, every N (1.04-2.2x the group kernel); binary32 one-butterfly
+// sizes, every N except, where the persistent bulk-copy kernel takes the plan (back-to-back
+// lines, N even), N = 2, 4, 6, 10 and 12, which that kernel runs at 0.85-0.98 of HBM against
+// 0.74-0.86; binary32 two-pass sizes only where the bulk-copy kernel does not run (odd N or
+// other layouts: N = 21, 25, 27 take 0.45-0.56 ms against 0.76-0.78 on the group kernel, while
+// the bulk-copy kernel runs the even sizes faster, N = 32 in 0.47 ms against 0.68).
+static bool small_preferred(int prec, int64_t N, int npass, bool bulk_copy) {
   if (prec == 0) return true;
+  if (npass == 2) return !bulk_copy;
   return !(bulk_copy && (N == 2 || N == 4 || N == 6 || N == 10 || N == 12));
 }
 
@@ -609,8 +613,8 @@ std::string build_c2c(Plan& p, int64_t tile_target) {
   // group and bulk-copy kernels
   p.small_grid = 0;
   if (p.ngroups == 1 && p.howmany2 == 1 && p.stages.empty() && p.howmany > 0 && !p.cluster &&
-      !p.generic_kernels && !p.wait_give_up && small_enabled() && small_kernel_applies(g0) &&
-      small_preferred(prec, N, p.stream) && prepare_small_kernels() == cudaSuccess)
+      !p.generic_kernels && !p.wait_give_up && small_enabled() && small_kernel_applies(g0, prec) &&
+      small_preferred(prec, N, g0.npass, p.stream) && prepare_small_kernels() == cudaSuccess)
     p.small_grid = small_grid(g0, prec);
   if (prec == 1 && !p.stream && p.howmany > 0) {
     // three tile buffers per CTA (stage + two work buffers): shrink C to fit

@@ -56,20 +56,26 @@ __device__ __forceinline__ int small_slot(int t, int r) {
   else return r;
 }
 
-// binary64 R <= 8: three CTAs per SM (80 registers, no spills; more loads in flight); binary64
-// R = 16: one (224 registers; at 128 it spills, and 4 % slower than the group kernel, 1.163
-// against 1.213 ms for 2^22 lines); else two
-template <class T, bool FWD, int R>
+// The kernel for a plan of radix R0 (R1 = 1), or of radices R0 then R1 (binary32, N = R0 R1
+// <= 32 points: two passes, out of place between the warp's two tiles).  Binary64 R0 <= 8:
+// three CTAs per SM (80 registers, no spills; more loads in flight); binary64 R0 = 16: one (224
+// registers; at 128 it spills, and 4 % slower than the group kernel, 1.163 against 1.213 ms
+// for 2^22 lines); else two.
+template <class T, bool FWD, int R0, int R1>
 __global__ void __launch_bounds__(kSmallThreads,
-                                  (sizeof(T) == 8 && R <= 8) ? 3 : (sizeof(T) == 8 && R == 16) ? 1 : 2)
+                                  (sizeof(T) == 8 && R0 <= 8) ? 3 : (sizeof(T) == 8 && R0 == 16) ? 1 : 2)
 small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>::C* out) {
   using P = Prec<T>;
   using Cx = typename P::C;
+  constexpr int R = R0 * R1;   // points per transform
   constexpr int K = small_k(R, (int)sizeof(Cx)), TPW = 32 * K, PT = small_pitch(R, (int)sizeof(Cx));
   constexpr int U = 128 / (int)sizeof(Cx);
+  constexpr int NT = R1 > 1 ? 2 : 1;   // tiles per warp
   extern __shared__ double2 small_smem[];
   const int lane = threadIdx.x & 31;
-  Cx* const tile = reinterpret_cast<Cx*>(small_smem) + (threadIdx.x >> 5) * (TPW * PT);
+  Cx* const tile = reinterpret_cast<Cx*>(small_smem) + (threadIdx.x >> 5) * (NT * TPW * PT);
+  Cx* const tile2 = tile + (NT - 1) * TPW * PT;   // the second tile of a two-pass plan
+  const Cx* __restrict__ tw1 = static_cast<const Cx*>(g.pass[R1 > 1 ? 1 : 0].tw);
   const int64_t ntr = g.total_sub;
   const int64_t nchunks = (ntr + TPW - 1) / TPW;
   const int64_t wstride = (int64_t)gridDim.x * kSmallWarps;
@@ -105,18 +111,61 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
     for (int k = 0; k < K; ++k) {
       const int t = k * 32 + lane;
       Cx* const v = tile + t * PT;
-      T x[2 * R], y[2 * R];
+      if constexpr (R1 == 1) {
+        T x[2 * R], y[2 * R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const Cx a = v[small_slot<R, U>(t, r)];
-        x[2 * r] = a.x;
-        x[2 * r + 1] = a.y;
+        for (int r = 0; r < R; ++r) {
+          const Cx a = v[small_slot<R, U>(t, r)];
+          x[2 * r] = a.x;
+          x[2 * r + 1] = a.y;
+        }
+        P::template Bfly<FWD, R, false>::run(x, y, one, nz);
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          v[small_slot<R, U>(t, r)] = unit ? P::mk(y[2 * r], y[2 * r + 1])
+                                           : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
+      } else {
+        // the plan's two Stockham passes on the lane's own transform, one butterfly at a
+        // time: pass 0 (radix R0, no twiddles) butterfly j reads elements j + r R1 of the
+        // first tile and writes j R0 + r of the second; pass 1 (radix R1, ns = R0) butterfly
+        // kk reads kk + r R0 of the second tile, with twiddle w_r(kk) at table entry
+        // (r - 1) R0 + kk, and writes kk + r R0 of the first
+        Cx* const v2 = tile2 + t * PT;
+#pragma unroll 1
+        for (int j = 0; j < R1; ++j) {
+          T x[2 * R0], y[2 * R0];
+#pragma unroll
+          for (int r = 0; r < R0; ++r) {
+            const Cx a = v[j + r * R1];
+            x[2 * r] = a.x;
+            x[2 * r + 1] = a.y;
+          }
+          P::template Bfly<FWD, R0, false>::run(x, y, one, nz);
+#pragma unroll
+          for (int r = 0; r < R0; ++r) v2[j * R0 + r] = P::mk(y[2 * r], y[2 * r + 1]);
+        }
+#pragma unroll 1
+        for (int kk = 0; kk < R0; ++kk) {
+          T x[4 * R1 - 2], y[2 * R1];
+#pragma unroll
+          for (int r = 0; r < R1; ++r) {
+            const Cx a = v2[kk + r * R0];
+            x[2 * r] = a.x;
+            x[2 * r + 1] = a.y;
+          }
+#pragma unroll
+          for (int r = 1; r < R1; ++r) {
+            const Cx w = __ldg(tw1 + (r - 1) * R0 + kk);
+            x[2 * R1 + 2 * (r - 1)] = w.x;
+            x[2 * R1 + 2 * (r - 1) + 1] = w.y;
+          }
+          P::template Bfly<FWD, R1, true>::run(x, y, one, nz);
+#pragma unroll
+          for (int r = 0; r < R1; ++r)
+            v[kk + r * R0] = unit ? P::mk(y[2 * r], y[2 * r + 1])
+                                  : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
+        }
       }
-      P::template Bfly<FWD, R, false>::run(x, y, one, nz);
-#pragma unroll
-      for (int r = 0; r < R; ++r)
-        v[small_slot<R, U>(t, r)] = unit ? P::mk(y[2 * r], y[2 * r + 1])
-                                         : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
     }
     __syncwarp();
     if (out_packed) {
@@ -139,73 +188,123 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
 }
 
 template <class T>
-size_t small_smem(int R) {
+size_t small_smem(int R, int tiles) {
   constexpr int es = (int)sizeof(typename Prec<T>::C);
-  return (size_t)kSmallWarps * 32 * small_k(R, es) * small_pitch(R, es) * es;
+  return (size_t)kSmallWarps * tiles * 32 * small_k(R, es) * small_pitch(R, es) * es;
 }
+
+// Two-pass binary32 plans with a compiled variant: the planner's radix pairs for the
+// 13-smooth sizes 18 .. 32
+constexpr int kSmallPairs[][2] = {{6, 3}, {10, 2}, {7, 3}, {11, 2}, {12, 2}, {5, 5},
+                                  {13, 2}, {9, 3}, {14, 2}, {15, 2}, {16, 2}};
 
 template <class T, bool FWD>
-const void* small_fn(int R) {
-  switch (R) {
+const void* small_fn(int R0, int R1) {
+  if (R1 == 1) {
+    switch (R0) {
 #define LFG_SMALL_CASE(RR) \
-  case RR: return (const void*)small_kernel<T, FWD, RR>;
-    LFG_SMALL_CASE(2)
-    LFG_SMALL_CASE(3)
-    LFG_SMALL_CASE(4)
-    LFG_SMALL_CASE(5)
-    LFG_SMALL_CASE(6)
-    LFG_SMALL_CASE(7)
-    LFG_SMALL_CASE(8)
-    LFG_SMALL_CASE(9)
-    LFG_SMALL_CASE(10)
-    LFG_SMALL_CASE(11)
-    LFG_SMALL_CASE(12)
-    LFG_SMALL_CASE(13)
-    LFG_SMALL_CASE(14)
-    LFG_SMALL_CASE(15)
-    LFG_SMALL_CASE(16)
+  case RR: return (const void*)small_kernel<T, FWD, RR, 1>;
+      LFG_SMALL_CASE(2)
+      LFG_SMALL_CASE(3)
+      LFG_SMALL_CASE(4)
+      LFG_SMALL_CASE(5)
+      LFG_SMALL_CASE(6)
+      LFG_SMALL_CASE(7)
+      LFG_SMALL_CASE(8)
+      LFG_SMALL_CASE(9)
+      LFG_SMALL_CASE(10)
+      LFG_SMALL_CASE(11)
+      LFG_SMALL_CASE(12)
+      LFG_SMALL_CASE(13)
+      LFG_SMALL_CASE(14)
+      LFG_SMALL_CASE(15)
+      LFG_SMALL_CASE(16)
 #undef LFG_SMALL_CASE
-    default: return nullptr;
+      default: return nullptr;
+    }
   }
+  if constexpr (sizeof(T) == 4) {
+#define LFG_SMALL_PAIR(A, B) \
+  if (R0 == A && R1 == B) return (const void*)small_kernel<T, FWD, A, B>;
+    LFG_SMALL_PAIR(6, 3)
+    LFG_SMALL_PAIR(10, 2)
+    LFG_SMALL_PAIR(7, 3)
+    LFG_SMALL_PAIR(11, 2)
+    LFG_SMALL_PAIR(12, 2)
+    LFG_SMALL_PAIR(5, 5)
+    LFG_SMALL_PAIR(13, 2)
+    LFG_SMALL_PAIR(9, 3)
+    LFG_SMALL_PAIR(14, 2)
+    LFG_SMALL_PAIR(15, 2)
+    LFG_SMALL_PAIR(16, 2)
+#undef LFG_SMALL_PAIR
+  }
+  return nullptr;
 }
 
-const void* small_kernel_fn(int precision, bool fwd, int R) {
-  if (precision == 0) return fwd ? small_fn<double, true>(R) : small_fn<double, false>(R);
-  return fwd ? small_fn<float, true>(R) : small_fn<float, false>(R);
+const void* small_kernel_fn(int precision, bool fwd, int R0, int R1) {
+  if (precision == 0) return fwd ? small_fn<double, true>(R0, R1) : small_fn<double, false>(R0, R1);
+  return fwd ? small_fn<float, true>(R0, R1) : small_fn<float, false>(R0, R1);
 }
 
-size_t small_smem_bytes(int precision, int R) {
-  return precision == 0 ? small_smem<double>(R) : small_smem<float>(R);
+size_t small_smem_bytes(int precision, int R0, int R1) {
+  const int tiles = R1 > 1 ? 2 : 1;
+  return precision == 0 ? small_smem<double>(R0 * R1, tiles) : small_smem<float>(R0 * R1, tiles);
+}
+
+// The radices of group g when the warp-tile kernel has a variant for its plan (r1 = 1: one
+// pass), else false.
+bool small_radices(const GroupDesc& g, int precision, int* r0, int* r1) {
+  if (g.nsub != 1 || g.total_sub <= 0 || g.M < 2) return false;
+  if (g.npass == 1 && g.M <= kSmallMaxN && g.pass[0].R == g.M && !g.pass[0].tw) {
+    *r0 = g.M;
+    *r1 = 1;
+    return true;
+  }
+  const PassDesc &a = g.pass[0], &b = g.pass[1];
+  if (g.npass == 2 && precision == 1 && g.M <= kSmallMaxTwoPassN && !a.tw && b.tw && !b.comp &&
+      a.R * b.R == g.M && b.ns_loc == a.R && b.ns_g == a.R && small_kernel_fn(1, true, a.R, b.R)) {
+    *r0 = a.R;
+    *r1 = b.R;
+    return true;
+  }
+  return false;
 }
 
 }  // namespace
 
-bool small_kernel_applies(const GroupDesc& g) {
-  return g.npass == 1 && g.nsub == 1 && g.M >= 2 && g.M <= kSmallMaxN && g.pass[0].R == g.M &&
-         g.pass[0].tw == nullptr && g.total_sub > 0;
+bool small_kernel_applies(const GroupDesc& g, int precision) {
+  int r0 = 0, r1 = 0;
+  return small_radices(g, precision, &r0, &r1);
 }
 
 cudaError_t prepare_small_kernels() {
   for (int prec = 0; prec < 2; ++prec)
-    for (int fwd = 0; fwd < 2; ++fwd)
-      for (int R = 2; R <= kSmallMaxN; ++R) {
-        const size_t s = small_smem_bytes(prec, R);
-        if (s <= 48 * 1024) continue;
-        cudaError_t e = cudaFuncSetAttribute(small_kernel_fn(prec, fwd != 0, R),
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s);
-        if (e != cudaSuccess) return e;
-      }
+    for (int fwd = 0; fwd < 2; ++fwd) {
+      auto allow = [&](int r0, int r1) -> cudaError_t {
+        const void* fn = small_kernel_fn(prec, fwd != 0, r0, r1);
+        const size_t s = small_smem_bytes(prec, r0, r1);
+        if (!fn || s <= 48 * 1024) return cudaSuccess;
+        return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s);
+      };
+      for (int R = 2; R <= kSmallMaxN; ++R)
+        if (cudaError_t e = allow(R, 1)) return e;
+      for (const auto& pr : kSmallPairs)
+        if (cudaError_t e = allow(pr[0], pr[1])) return e;
+    }
   return cudaSuccess;
 }
 
 unsigned small_grid(const GroupDesc& g, int precision) {
+  int r0 = 0, r1 = 0;
+  if (!small_radices(g, precision, &r0, &r1)) return 0;
   const int R = g.M;
-  const void* fn = small_kernel_fn(precision, true, R);
+  const void* fn = small_kernel_fn(precision, true, r0, r1);
   int dev = 0, sms = 1, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSmallThreads,
-                                                    small_smem_bytes(precision, R)) != cudaSuccess ||
+                                                    small_smem_bytes(precision, r0, r1)) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
   const int64_t tpb = (int64_t)kSmallWarps * 32 * small_k(R, precision == 0 ? 16 : 8);
@@ -215,14 +314,14 @@ unsigned small_grid(const GroupDesc& g, int precision) {
 
 cudaError_t launch_small(const GroupDesc& gd, int precision, bool fwd, const void* in, void* out,
                          unsigned grid, cudaStream_t stream) {
-  if (!small_kernel_applies(gd)) return cudaErrorInvalidValue;
+  int r0 = 0, r1 = 0;
+  if (!small_radices(gd, precision, &r0, &r1)) return cudaErrorInvalidValue;
   GroupDesc g = gd;
   set_divisors(g);
-  const int R = g.M;
-  const size_t smem = small_smem_bytes(precision, R);
+  const size_t smem = small_smem_bytes(precision, r0, r1);
   void* args[] = {(void*)&g, (void*)&in, (void*)&out};
-  return cudaLaunchKernel(small_kernel_fn(precision, fwd, R), dim3(grid), dim3(kSmallThreads), args,
-                          smem, stream);
+  return cudaLaunchKernel(small_kernel_fn(precision, fwd, r0, r1), dim3(grid), dim3(kSmallThreads),
+                          args, smem, stream);
 }
 
 }  // namespace lfg

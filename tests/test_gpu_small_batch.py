@@ -1,7 +1,8 @@
-"""Batched one-butterfly sizes (N = 2 .. 16) on the warp-tile kernel (csrc/small.cu).
+"""Batched small sizes on the warp-tile kernel (csrc/small.cu).
 
 A plan of N <= 16 points is one untwiddled codelet per transform; the warp-tile kernel runs
-it with per-warp shared-memory chunks instead of the CTA-wide tile of the group kernels.  Its
+it with per-warp shared-memory chunks instead of the CTA-wide tile of the group kernels, and
+it runs the two passes of binary32 plans of up to 32 points between two warp tiles.  Its
 results must be the bits of the reference transform (binary64: the oracle's refTransform for
 the plan's radix sequence; both precisions: the group kernels, LFG_GENERIC_KERNELS), for
 batches that leave a partial last chunk, in place, scaled, and over gapped and transposed
@@ -123,3 +124,35 @@ def test_small_sizes_f32_gapped_equal_bulk_copy(n):
     assert packed.info().small_kernel == 0
     ref = packed.execute(torch.from_numpy(x).cuda()).cpu().numpy()
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), n
+
+
+@pytest.mark.parametrize("n", [18, 20, 21, 22, 24, 25, 26, 27, 28, 30, 32])
+def test_two_pass_f32_sizes(n):
+    """Binary32 two-pass sizes up to 32: odd sizes over back-to-back lines, and every size over
+    gapped lines, run on the warp-tile kernel (even sizes over back-to-back lines take the
+    bulk-copy kernel); all give the group kernels' bits, in place too, and scaled."""
+    B = 1000 + n
+    x = O.uniform_complex((B, n), seed=50 + n).astype(np.complex64)
+    xd = torch.from_numpy(x).cuda()
+    d = n + 1
+    buf = np.zeros((B, d), dtype=np.complex64)
+    buf[:, :n] = x
+    for sign in (-1, 1):
+        ref = lfg.plan_1d(n, sign, B, precision="f32", generic_kernels=True).execute(xd)
+        plan = lfg.plan_1d(n, sign, B, precision="f32")
+        assert plan.info().small_kernel == n % 2, n
+        assert _bits_equal(plan.execute(xd), ref), (n, sign)
+        inplace = xd.clone()
+        plan.execute(inplace, inplace)
+        assert _bits_equal(inplace, ref), (n, sign)
+        spec = [0, sign, 1, 1, 0, 1, 0, 1, n, 2, 2, B, 2 * d, 2 * d]
+        gapped = lfg.plan_spec(spec, precision="f32")
+        assert gapped.info().small_kernel == 1
+        xin = torch.from_numpy(buf.reshape(-1).view(np.float32).copy()).cuda()
+        out = torch.zeros(2 * B * d, dtype=torch.float32, device="cuda")
+        gapped.execute(xin, out)
+        got = np.ascontiguousarray(out.cpu().numpy().view(np.complex64).reshape(B, d)[:, :n])
+        assert np.array_equal(got.view(np.uint32), ref.cpu().numpy().view(np.uint32)), (n, sign)
+    scaled = lfg.plan_1d(n, 1, B, precision="f32").set_scale(1.0 / n)
+    gen = lfg.plan_1d(n, 1, B, precision="f32", generic_kernels=True).set_scale(1.0 / n)
+    assert _bits_equal(scaled.execute(xd), gen.execute(xd)), n
