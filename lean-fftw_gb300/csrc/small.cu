@@ -1,23 +1,25 @@
-// Batched one-butterfly transforms: N = R <= 16 points, a single untwiddled pass.
+// Batched small transforms: one-butterfly sizes (N = R <= 16 points, a single untwiddled pass)
+// in both precisions, and binary32 plans of two passes up to 32 points.
 //
-// A plan of such a size is one codelet per transform, so its kernel is a copy with a little
+// A one-butterfly plan is one codelet per transform, so its kernel is a copy with a little
 // arithmetic: memory-bound in binary32, and in binary64 bound by memory for N <= 4 and by the
 // FP64 pipe above.  The shared-memory group kernel moves each byte through a CTA-wide tile
 // and two barriers per tile, which leaves these sizes at 35-60 % of HBM.  Here each warp works
 // on its own chunk of transforms with warp-level synchronisation only:
 //
-//   1. the chunk (32 K transforms, K = 256 / (R x element bytes), so that every lane has about
-//      256 bytes in flight) is read with coalesced loads -- consecutive lanes take consecutive elements
-//      of a transform when elements are contiguous, else the same element of consecutive
-//      transforms -- into the warp's tile (layout: small_slot below, conflict-free for the
-//      staging and for the lane-strided reads and writes of step 2);
-//   2. each lane runs the codelet on K transforms of the tile, in place (scaled on the way
-//      out when the plan's scale is not 1, as the group kernel's stores do);
+//   1. the chunk (32 K transforms, K = 256 / (N x element bytes), so that every lane has about
+//      256 bytes in flight) is read with coalesced loads -- consecutive lanes take consecutive
+//      elements of a transform when elements are contiguous, else the same element of
+//      consecutive transforms -- into the warp's tile (layout: small_slot below,
+//      conflict-free for the staging and for the lane-strided reads and writes of step 2);
+//   2. each lane runs the plan on K transforms of the tile: the codelet in place (scaled on
+//      the way out when the plan's scale is not 1, as the group kernel's stores do), or the
+//      two passes between the warp's two tiles;
 //   3. the chunk is written back with the loads' ordering.
 //
-// The butterflies are the generated codelets of the group kernels, so the results are the
-// same bits.  In place is safe: a warp reads its whole chunk before it writes any of it, and
-// chunks are disjoint.
+// The butterflies are the generated codelets of the group kernels and the passes follow the
+// same Stockham schedule, so the results are the same bits.  In place is safe: a warp reads
+// its whole chunk before it writes any of it, and chunks are disjoint.
 #include <cuda_runtime.h>
 
 #include <algorithm>
