@@ -12,7 +12,8 @@ Workloads (synthetic inputs, re/im iid uniform[-0.5, 0.5) from numpy default_rng
              (`per_size`) and spread over 64 independent graph branches so that different
              sizes run at the same time (`per_size_concurrent`).
   c2c_<N>    1-D complex FP64 forward, N = 2^k (k = 1..18), batch 2^26 / N (1 GiB in and
-             out): the power-of-two sweep.
+             out): the power-of-two sweep; also the small sizes N = 3, 5, 6, 7, 9 .. 15, 21,
+             25, 27 (batch floor(2^26 / N)).
   small_1024 one transform of N = 1024 (the plain small case: latency-bound).
   large_262144[_f32]  32 transforms of N = 2^18, binary64 (or binary32: the FP32 variant with
              compensated last-pass twiddles).
@@ -58,6 +59,9 @@ SEED = 20261016
 WORKLOADS = {"ragged": dict(kind="ragged", count=8192, sign=-1)}
 for _k in range(1, 19):
     WORKLOADS[f"c2c_{1 << _k}"] = dict(kind="c2c", n=1 << _k, batch=(1 << 26) >> _k, sign=-1)
+# small sizes that are not powers of two (one butterfly, or two passes): 1 GiB in and out
+for _n in (3, 5, 6, 7, 9, 10, 11, 12, 13, 14, 15, 21, 25, 27):
+    WORKLOADS[f"c2c_{_n}"] = dict(kind="c2c", n=_n, batch=(1 << 26) // _n, sign=-1)
 # the other configurations of the reference's measurement plan, each as its own line
 WORKLOADS.update({
     "small_1024": dict(kind="c2c", n=1024, batch=1, sign=-1),           # latency-bound
