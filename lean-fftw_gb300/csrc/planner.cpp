@@ -45,14 +45,15 @@ static bool small_enabled() {
 // Where the warp-tile kernel runs a plan it has a variant for, from 1 GiB batches on GB300:
 // binary64 one-butterfly sizes, every N (1.04-2.2x the group kernel); binary32 one-butterfly
 // sizes, every N except, where the persistent bulk-copy kernel takes the plan (back-to-back
-// lines, N even), N = 2, 4, 6, 10 and 12, which that kernel runs at 0.85-0.98 of HBM against
-// 0.74-0.86; binary32 two-pass sizes only where the bulk-copy kernel does not run (odd N or
-// other layouts: N = 21, 25, 27 take 0.45-0.56 ms against 0.76-0.78 on the group kernel, while
-// the bulk-copy kernel runs the even sizes faster, N = 32 in 0.47 ms against 0.68).
+// lines, N even), N = 2, 4 and 12, which that kernel runs at 0.92-0.98 of HBM against
+// 0.89-0.98 (N = 6 and 10: 0.92-0.93 against 0.86-0.87); binary32 two-pass sizes only where the
+// bulk-copy kernel does not run (odd N or other layouts: N = 21, 25, 27 take 0.45-0.56 ms
+// against 0.76-0.78 on the group kernel, while the bulk-copy kernel runs the even sizes faster,
+// N = 32 in 0.47 ms against 0.68).
 static bool small_preferred(int prec, int64_t N, int npass, bool bulk_copy) {
   if (prec == 0) return true;
   if (npass == 2) return !bulk_copy;
-  return !(bulk_copy && (N == 2 || N == 4 || N == 6 || N == 10 || N == 12));
+  return !(bulk_copy && (N == 2 || N == 4 || N == 12));
 }
 
 namespace {

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "kernels.h"
 #include "stockham_dev.cuh"
@@ -189,6 +190,115 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
   }
 }
 
+// Pipelined variant of the one-pass kernel: the warp's chunks are staged by asynchronous
+// copies (cp.async, no registers held) into two tiles in turn, so that the next chunk is in
+// flight while the current one is computed and stored; chunks of half the size keep the
+// shared memory per warp.
+__device__ __forceinline__ void small_cp_async(void* dst, const void* src, int bytes) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if (bytes == 16)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+
+template <class T, bool FWD, int R>
+__global__ void __launch_bounds__(kSmallThreads,
+                                  (sizeof(T) == 8 && R <= 8) ? 3 : (sizeof(T) == 8 && R == 16) ? 1 : 2)
+small_kernel_pipe(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>::C* out) {
+  using P = Prec<T>;
+  using Cx = typename P::C;
+  constexpr int KF = small_k(R, (int)sizeof(Cx));
+  constexpr int K = KF > 1 ? KF / 2 : 1, TPW = 32 * K, PT = small_pitch(R, (int)sizeof(Cx));
+  constexpr int U = 128 / (int)sizeof(Cx);
+  extern __shared__ double2 small_smem[];
+  const int lane = threadIdx.x & 31;
+  Cx* const tiles = reinterpret_cast<Cx*>(small_smem) + (threadIdx.x >> 5) * (2 * TPW * PT);
+  const int64_t ntr = g.total_sub;
+  const int64_t nchunks = (ntr + TPW - 1) / TPW;
+  const int64_t wstride = (int64_t)gridDim.x * kSmallWarps;
+  const int64_t il = g.in_line, ie = g.in_elem, ol = g.out_line, oe = g.out_elem;
+  const bool in_rfast = ie == 1, out_rfast = oe == 1;
+  const bool in_packed = in_rfast && il == R, out_packed = out_rfast && ol == R;
+  const bool unit = g.unit_scale != 0;
+  const T sc = sizeof(T) == 4 ? (T)g.scale_f32 : (T)g.scale;
+  T one, nz;
+  P::units(one, nz);
+  auto issue = [&](int64_t ch, Cx* tile) {
+    const int64_t t0 = ch * TPW;
+    const int nt = (int)min((int64_t)TPW, ntr - t0);
+    const Cx* src = in + t0 * il;
+    if (in_packed) {
+#pragma unroll
+      for (int k = 0; k < R * K; ++k) {
+        const int e = k * 32 + lane;
+        if (e < nt * R)
+          small_cp_async(tile + (e / R) * PT + small_slot<R, U>(e / R, e % R), src + e, (int)sizeof(Cx));
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < R * K; ++k) {
+        const int e = k * 32 + lane;
+        const int t = in_rfast ? e / R : e % TPW;
+        const int r = in_rfast ? e - t * R : e / TPW;
+        if (t < nt)
+          small_cp_async(tile + t * PT + small_slot<R, U>(t, r), src + (int64_t)t * il + (int64_t)r * ie,
+                         (int)sizeof(Cx));
+      }
+    }
+  };
+  int64_t ch = (int64_t)blockIdx.x * kSmallWarps + (threadIdx.x >> 5);
+  int b = 0;
+  if (ch < nchunks) issue(ch, tiles);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  for (; ch < nchunks; ch += wstride) {
+    Cx* const tile = tiles + b * (TPW * PT);
+    if (ch + wstride < nchunks) issue(ch + wstride, tiles + (b ^ 1) * (TPW * PT));
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 1;" ::: "memory");   // this chunk's copies have landed
+    __syncwarp();
+    const int64_t t0 = ch * TPW;
+    const int nt = (int)min((int64_t)TPW, ntr - t0);
+#pragma unroll 1
+    for (int k = 0; k < K; ++k) {
+      const int t = k * 32 + lane;
+      Cx* const v = tile + t * PT;
+      T x[2 * R], y[2 * R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const Cx a = v[small_slot<R, U>(t, r)];
+        x[2 * r] = a.x;
+        x[2 * r + 1] = a.y;
+      }
+      P::template Bfly<FWD, R, false>::run(x, y, one, nz);
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        v[small_slot<R, U>(t, r)] = unit ? P::mk(y[2 * r], y[2 * r + 1])
+                                         : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
+    }
+    __syncwarp();
+    Cx* dst = out + t0 * ol;
+    if (out_packed) {
+#pragma unroll
+      for (int k = 0; k < R * K; ++k) {
+        const int e = k * 32 + lane;
+        if (e < nt * R) dst[e] = tile[(e / R) * PT + small_slot<R, U>(e / R, e % R)];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < R * K; ++k) {
+        const int e = k * 32 + lane;
+        const int t = out_rfast ? e / R : e % TPW;
+        const int r = out_rfast ? e - t * R : e / TPW;
+        if (t < nt) dst[(int64_t)t * ol + (int64_t)r * oe] = tile[t * PT + small_slot<R, U>(t, r)];
+      }
+    }
+    __syncwarp();   // this tile is refilled by the chunk after next
+    b ^= 1;
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 template <class T>
 size_t small_smem(int R, int tiles) {
   constexpr int es = (int)sizeof(typename Prec<T>::C);
@@ -254,6 +364,49 @@ size_t small_smem_bytes(int precision, int R0, int R1) {
   return precision == 0 ? small_smem<double>(R0 * R1, tiles) : small_smem<float>(R0 * R1, tiles);
 }
 
+// One-pass plans run the pipelined variant (1 GiB batches on GB300: binary32 0.90-0.93 of HBM
+// against 0.80-0.91, binary64 N = 2 .. 12 and 16 up to 11 % faster), except binary64 R = 13 ..
+// 15, which measured 5-7 % slower pipelined; LFG_SMALL_PIPE=0 in the environment turns it off
+// (for comparisons; the same bits).
+bool small_pipe(int precision, int r0, int r1) {
+  if (r1 > 1 || (precision == 0 && r0 >= 13 && r0 <= 15)) return false;
+  const char* s = std::getenv("LFG_SMALL_PIPE");
+  return !(s && s[0] == '0');
+}
+
+size_t small_pipe_smem_bytes(int precision, int R) {
+  const int es = precision == 0 ? 16 : 8;
+  const int kf = small_k(R, es), k = kf > 1 ? kf / 2 : 1;
+  return (size_t)kSmallWarps * 2 * 32 * k * small_pitch(R, es) * es;
+}
+
+const void* small_pipe_fn(int precision, bool fwd, int R) {
+  switch (R * 4 + precision * 2 + (fwd ? 1 : 0)) {
+#define LFG_PIPE_CASE(RR)                                                   \
+  case RR * 4 + 0: return (const void*)small_kernel_pipe<double, false, RR>; \
+  case RR * 4 + 1: return (const void*)small_kernel_pipe<double, true, RR>;  \
+  case RR * 4 + 2: return (const void*)small_kernel_pipe<float, false, RR>;  \
+  case RR * 4 + 3: return (const void*)small_kernel_pipe<float, true, RR>;
+    LFG_PIPE_CASE(2)
+    LFG_PIPE_CASE(3)
+    LFG_PIPE_CASE(4)
+    LFG_PIPE_CASE(5)
+    LFG_PIPE_CASE(6)
+    LFG_PIPE_CASE(7)
+    LFG_PIPE_CASE(8)
+    LFG_PIPE_CASE(9)
+    LFG_PIPE_CASE(10)
+    LFG_PIPE_CASE(11)
+    LFG_PIPE_CASE(12)
+    LFG_PIPE_CASE(13)
+    LFG_PIPE_CASE(14)
+    LFG_PIPE_CASE(15)
+    LFG_PIPE_CASE(16)
+#undef LFG_PIPE_CASE
+    default: return nullptr;
+  }
+}
+
 // The radices of group g when the warp-tile kernel has a variant for its plan (r1 = 1: one
 // pass), else false.
 bool small_radices(const GroupDesc& g, int precision, int* r0, int* r1) {
@@ -289,8 +442,14 @@ cudaError_t prepare_small_kernels() {
         if (!fn || s <= 48 * 1024) return cudaSuccess;
         return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s);
       };
-      for (int R = 2; R <= kSmallMaxN; ++R)
+      for (int R = 2; R <= kSmallMaxN; ++R) {
         if (cudaError_t e = allow(R, 1)) return e;
+        const size_t sp = small_pipe_smem_bytes(prec, R);
+        if (sp > 48 * 1024)
+          if (cudaError_t e = cudaFuncSetAttribute(small_pipe_fn(prec, fwd != 0, R),
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp))
+            return e;
+      }
       for (const auto& pr : kSmallPairs)
         if (cudaError_t e = allow(pr[0], pr[1])) return e;
     }
@@ -301,15 +460,17 @@ unsigned small_grid(const GroupDesc& g, int precision) {
   int r0 = 0, r1 = 0;
   if (!small_radices(g, precision, &r0, &r1)) return 0;
   const int R = g.M;
-  const void* fn = small_kernel_fn(precision, true, r0, r1);
+  const bool pipe = small_pipe(precision, r0, r1);
+  const void* fn = pipe ? small_pipe_fn(precision, true, R) : small_kernel_fn(precision, true, r0, r1);
+  const size_t smem = pipe ? small_pipe_smem_bytes(precision, R) : small_smem_bytes(precision, r0, r1);
   int dev = 0, sms = 1, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSmallThreads,
-                                                    small_smem_bytes(precision, r0, r1)) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSmallThreads, smem) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
-  const int64_t tpb = (int64_t)kSmallWarps * 32 * small_k(R, precision == 0 ? 16 : 8);
+  const int kf = small_k(R, precision == 0 ? 16 : 8);
+  const int64_t tpb = (int64_t)kSmallWarps * 32 * (pipe ? (kf > 1 ? kf / 2 : 1) : kf);
   const int64_t need = (g.total_sub + tpb - 1) / tpb;
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sms * per_sm));
 }
@@ -320,10 +481,11 @@ cudaError_t launch_small(const GroupDesc& gd, int precision, bool fwd, const voi
   if (!small_radices(gd, precision, &r0, &r1)) return cudaErrorInvalidValue;
   GroupDesc g = gd;
   set_divisors(g);
-  const size_t smem = small_smem_bytes(precision, r0, r1);
+  const bool pipe = small_pipe(precision, r0, r1);
+  const size_t smem = pipe ? small_pipe_smem_bytes(precision, g.M) : small_smem_bytes(precision, r0, r1);
   void* args[] = {(void*)&g, (void*)&in, (void*)&out};
-  return cudaLaunchKernel(small_kernel_fn(precision, fwd, r0, r1), dim3(grid), dim3(kSmallThreads),
-                          args, smem, stream);
+  return cudaLaunchKernel(pipe ? small_pipe_fn(precision, fwd, g.M) : small_kernel_fn(precision, fwd, r0, r1),
+                          dim3(grid), dim3(kSmallThreads), args, smem, stream);
 }
 
 }  // namespace lfg

@@ -25,10 +25,10 @@ SIZES = list(range(2, 17))
 
 def _expect_small(n, precision):
     """The planner's choice for back-to-back lines: binary64 every N; binary32 all but the
-    sizes the bulk-copy kernel runs faster (N = 2, 4, 6, 10, 12)."""
+    sizes the bulk-copy kernel runs faster (N = 2, 4, 12)."""
     if precision == "f64":
         return 1
-    return int(n not in (2, 4, 6, 10, 12))
+    return int(n not in (2, 4, 12))
 
 
 def _bits_equal(a, b):
@@ -104,7 +104,7 @@ def test_small_sizes_strided_layouts(n):
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64)), n
 
 
-@pytest.mark.parametrize("n", [2, 4, 6, 10, 12])
+@pytest.mark.parametrize("n", [2, 4, 12])
 def test_small_sizes_f32_gapped_equal_bulk_copy(n):
     """The binary32 sizes that the bulk-copy kernel takes over back-to-back lines run on the
     warp-tile kernel over gapped lines: the same bits."""
@@ -156,3 +156,17 @@ def test_two_pass_f32_sizes(n):
     scaled = lfg.plan_1d(n, 1, B, precision="f32").set_scale(1.0 / n)
     gen = lfg.plan_1d(n, 1, B, precision="f32", generic_kernels=True).set_scale(1.0 / n)
     assert _bits_equal(scaled.execute(xd), gen.execute(xd)), n
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("n", [2, 3, 8, 16])
+def test_small_pipelined_equals_plain(n, precision, monkeypatch):
+    """One-pass plans run the pipelined variant (asynchronous copies into two tiles per warp);
+    the unpipelined one (LFG_SMALL_PIPE=0) gives the same bits."""
+    B = 3001 + n
+    dt = torch.complex128 if precision == "f64" else torch.complex64
+    xd = torch.from_numpy(O.uniform_complex((B, n), seed=70 + n)).to("cuda", dt)
+    piped = lfg.plan_1d(n, -1, B, precision=precision).execute(xd)
+    monkeypatch.setenv("LFG_SMALL_PIPE", "0")
+    plain = lfg.plan_1d(n, -1, B, precision=precision).execute(xd)
+    assert _bits_equal(piped, plain), (n, precision)
