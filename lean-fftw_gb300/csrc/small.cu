@@ -59,6 +59,52 @@ __device__ __forceinline__ int small_slot(int t, int r) {
   else return r;
 }
 
+// Lane work of a one-pass plan: the codelet on transform t of the tile, in place (scaled on the
+// way out when the plan's scale is not 1, as the group kernel's stores do).
+template <class T, bool FWD, int R, int U, int PT>
+__device__ __forceinline__ void small_onepass(typename Prec<T>::C* tile, int t, T one, T nz, bool unit,
+                                              T sc) {
+  using P = Prec<T>;
+  using Cx = typename P::C;
+  Cx* const v = tile + t * PT;
+  T x[2 * R], y[2 * R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const Cx a = v[small_slot<R, U>(t, r)];
+    x[2 * r] = a.x;
+    x[2 * r + 1] = a.y;
+  }
+  P::template Bfly<FWD, R, false>::run(x, y, one, nz);
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    v[small_slot<R, U>(t, r)] = unit ? P::mk(y[2 * r], y[2 * r + 1])
+                                     : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
+}
+
+// The warp's stores of a chunk of nt transforms (K per lane) from its tile to dst, in the
+// loads' ordering: consecutive lanes on consecutive elements of a transform when the output's
+// elements are contiguous, else on the same element of consecutive transforms.
+template <int R, int U, int PT, int K, class Cx>
+__device__ __forceinline__ void small_store(const Cx* tile, Cx* dst, int nt, int lane, bool packed,
+                                            bool rfast, int64_t ol, int64_t oe) {
+  constexpr int TPW = 32 * K;
+  if (packed) {
+#pragma unroll
+    for (int k = 0; k < R * K; ++k) {
+      const int e = k * 32 + lane;
+      if (e < nt * R) dst[e] = tile[(e / R) * PT + small_slot<R, U>(e / R, e % R)];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < R * K; ++k) {
+      const int e = k * 32 + lane;
+      const int t = rfast ? e / R : e % TPW;
+      const int r = rfast ? e - t * R : e / TPW;
+      if (t < nt) dst[(int64_t)t * ol + (int64_t)r * oe] = tile[t * PT + small_slot<R, U>(t, r)];
+    }
+  }
+}
+
 // The kernel for a plan of radix R0 (R1 = 1), or of radices R0 then R1 (binary32, N = R0 R1
 // <= 32 points: two passes, out of place between the warp's two tiles).  Binary64 R0 <= 8:
 // three CTAs per SM (80 registers, no spills; more loads in flight); binary64 R0 = 16: one (224
@@ -113,21 +159,10 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
 #pragma unroll 1
     for (int k = 0; k < K; ++k) {
       const int t = k * 32 + lane;
-      Cx* const v = tile + t * PT;
       if constexpr (R1 == 1) {
-        T x[2 * R], y[2 * R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const Cx a = v[small_slot<R, U>(t, r)];
-          x[2 * r] = a.x;
-          x[2 * r + 1] = a.y;
-        }
-        P::template Bfly<FWD, R, false>::run(x, y, one, nz);
-#pragma unroll
-        for (int r = 0; r < R; ++r)
-          v[small_slot<R, U>(t, r)] = unit ? P::mk(y[2 * r], y[2 * r + 1])
-                                           : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
+        small_onepass<T, FWD, R, U, PT>(tile, t, one, nz, unit, sc);
       } else {
+        Cx* const v = tile + t * PT;
         // the plan's two Stockham passes on the lane's own transform, one butterfly at a
         // time: pass 0 (radix R0, no twiddles) butterfly j reads elements j + r R1 of the
         // first tile and writes j R0 + r of the second; pass 1 (radix R1, ns = R0) butterfly
@@ -171,21 +206,7 @@ small_kernel(const GroupDesc g, const typename Prec<T>::C* in, typename Prec<T>:
       }
     }
     __syncwarp();
-    if (out_packed) {
-#pragma unroll
-      for (int k = 0; k < R * K; ++k) {
-        const int e = k * 32 + lane;
-        if (e < nt * R) dst[e] = tile[(e / R) * PT + small_slot<R, U>(e / R, e % R)];
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < R * K; ++k) {
-        const int e = k * 32 + lane;
-        const int t = out_rfast ? e / R : e % TPW;
-        const int r = out_rfast ? e - t * R : e / TPW;
-        if (t < nt) dst[(int64_t)t * ol + (int64_t)r * oe] = tile[t * PT + small_slot<R, U>(t, r)];
-      }
-    }
+    small_store<R, U, PT, K>(tile, dst, nt, lane, out_packed, out_rfast, ol, oe);
     __syncwarp();   // the tile is refilled by the warp's next chunk
   }
 }
@@ -260,39 +281,9 @@ small_kernel_pipe(const GroupDesc g, const typename Prec<T>::C* in, typename Pre
     const int64_t t0 = ch * TPW;
     const int nt = (int)min((int64_t)TPW, ntr - t0);
 #pragma unroll 1
-    for (int k = 0; k < K; ++k) {
-      const int t = k * 32 + lane;
-      Cx* const v = tile + t * PT;
-      T x[2 * R], y[2 * R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const Cx a = v[small_slot<R, U>(t, r)];
-        x[2 * r] = a.x;
-        x[2 * r + 1] = a.y;
-      }
-      P::template Bfly<FWD, R, false>::run(x, y, one, nz);
-#pragma unroll
-      for (int r = 0; r < R; ++r)
-        v[small_slot<R, U>(t, r)] = unit ? P::mk(y[2 * r], y[2 * r + 1])
-                                         : P::mk(P::mul(y[2 * r], sc), P::mul(y[2 * r + 1], sc));
-    }
+    for (int k = 0; k < K; ++k) small_onepass<T, FWD, R, U, PT>(tile, k * 32 + lane, one, nz, unit, sc);
     __syncwarp();
-    Cx* dst = out + t0 * ol;
-    if (out_packed) {
-#pragma unroll
-      for (int k = 0; k < R * K; ++k) {
-        const int e = k * 32 + lane;
-        if (e < nt * R) dst[e] = tile[(e / R) * PT + small_slot<R, U>(e / R, e % R)];
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < R * K; ++k) {
-        const int e = k * 32 + lane;
-        const int t = out_rfast ? e / R : e % TPW;
-        const int r = out_rfast ? e - t * R : e / TPW;
-        if (t < nt) dst[(int64_t)t * ol + (int64_t)r * oe] = tile[t * PT + small_slot<R, U>(t, r)];
-      }
-    }
+    small_store<R, U, PT, K>(tile, out + t0 * ol, nt, lane, out_packed, out_rfast, ol, oe);
     __syncwarp();   // this tile is refilled by the chunk after next
     b ^= 1;
   }
